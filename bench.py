@@ -1,0 +1,346 @@
+"""Benchmark of the batched Kronecker matrix-vector product on GB300.
+
+Default workload: the plain FP64 forward at d=6, n=4 (N=4096), matrix_stride 8,
+4096 output vectors x fan-in 9 = 36864 entries, seeded synthetic data
+(factors U[-1,1], inputs N(0,1)).  One step = one kronmult_batched pass over the
+whole batch.  Prints one JSON line.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--config c1|c2|c4|c5] [--dtype f64|f32]
+
+value       GFLOP/s (algorithmic 2*d*n*N flops per entry) over K device-timed steps,
+            inputs resident in HBM (the 1.2 GB input set is 9x the 129 MB L2, so no
+            flush is needed between steps)
+e2e         the same metric through the public API with host (pinned) buffers:
+            each step copies the inputs and factors in and the outputs back
+roofline    the forward kernel against the roof that binds it; for FP64 that is the
+            FP64 FMA pipe, measured live (HBM fraction reported beside it)
+cpu_baseline  the C oracle (a restatement of the reference's kronmult_omp) on the
+            host cores, same workload
+--impl reference  the reference's CPU algorithm (oracle port; the reference sources are
+            not present on the GPU host) timed on all host cores
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIGS = {
+    "c1": ("config1", "fwd_d3_n4_b8192"),
+    "c2": ("config2", "fwd_d6_n4_b36864"),
+    "c4": ("config4", "fwd_d4_n8_b32768"),
+    "c5": ("config5", "fwdadj_d3_n6_b16384"),
+}
+METRIC = "kron-matvec GFLOP/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--config", choices=sorted(CONFIGS), default="c2")
+    p.add_argument("--dtype", choices=["f64", "f32"], default="f64")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--e2e-steps", type=int, default=5)
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_batch(cfg: str, rank: int):
+    from kronmult_gb300 import workloads as W
+
+    fn, _ = CONFIGS[cfg]
+    # weak scaling: every rank owns a full-size shard with its own seed (shards are
+    # whole output groups, so no data crosses ranks)
+    return getattr(W, fn)(seed=getattr(W, fn).__defaults__[1] + 7919 * rank)
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(b, dtype, budget_s: float = 15.0):
+    """Time the oracle (OpenMP, all host threads) on the workload, or on a bounded
+    prefix of its entries when the whole would take longer than ~budget_s."""
+    from oracle import oracle as O
+    from kronmult_gb300.workloads import Batch
+
+    threads = O.max_threads("port")
+    probe = min(b.nb, 2048)
+    sub = Batch(b.name, b.d, b.n, b.stride, b.block, b.factors, b.inputs[:probe], b.out_init,
+                b.fac_index[:probe], b.out_index[:probe])
+    t0 = time.perf_counter()
+    O.forward(sub, dtype=dtype)
+    t_probe = time.perf_counter() - t0
+    per_entry = t_probe / probe
+    count = int(min(b.nb, max(probe, budget_s / 3 / max(per_entry, 1e-12))))
+    sub = Batch(b.name, b.d, b.n, b.stride, b.block, b.factors, b.inputs[:count], b.out_init,
+                b.fac_index[:count], b.out_index[:count])
+    best = float("inf")
+    for _ in range(3):
+        t0 = time.perf_counter()
+        O.forward(sub, dtype=dtype)
+        best = min(best, time.perf_counter() - t0)
+    flops = 2.0 * b.d * b.n * b.N * count
+    return {"value": flops / best / 1e9, "unit": "GFLOP/s", "cores": threads, "kind": "port",
+            "sample": f"{count} of {b.nb} entries of the same batch, best of 3, {threads} OpenMP threads"}
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the reference's CPU algorithm on the host cores."""
+    if rank != 0:
+        return
+    b = make_batch(args.config, 0)
+    dt = np.float64 if args.dtype == "f64" else np.float32
+    from oracle import oracle as O
+    from kronmult_gb300.workloads import Batch
+
+    threads = O.max_threads("port")
+    # bounded sample per step so that warmup+steps stay within a few minutes
+    probe = min(b.nb, 1024)
+    sub = Batch(b.name, b.d, b.n, b.stride, b.block, b.factors, b.inputs[:probe], b.out_init,
+                b.fac_index[:probe], b.out_index[:probe])
+    t0 = time.perf_counter()
+    O.forward(sub, dtype=dt)
+    per_entry = (time.perf_counter() - t0) / probe
+    total_steps = args.steps + args.warmup
+    count = int(min(b.nb, max(64, 120.0 / total_steps / max(per_entry, 1e-12))))
+    sub = Batch(b.name, b.d, b.n, b.stride, b.block, b.factors, b.inputs[:count], b.out_init,
+                b.fac_index[:count], b.out_index[:count])
+    for _ in range(args.warmup):
+        O.forward(sub, dtype=dt)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        O.forward(sub, dtype=dt)
+    el = time.perf_counter() - t0
+    flops = 2.0 * b.d * b.n * b.N * count * args.steps
+    v = flops / el / 1e9
+    _, wname = CONFIGS[args.config]
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "GFLOP/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.dtype,
+        "data": "synthetic (seeded PCG64; factors U[-1,1], inputs N(0,1))",
+        "config": {"workload": wname, "d": b.d, "n": b.n, "matrix_stride": b.stride, "nb_batch": b.nb,
+                   "outputs": b.n_out, "sample_entries_per_step": count},
+        "cpu_baseline": {"value": v, "unit": "GFLOP/s", "cores": threads, "kind": "port",
+                         "sample": f"{count} of {b.nb} entries per step, {threads} OpenMP threads "
+                                   "(C restatement of kronmult_omp; the reference sources are not on this host)"},
+        "e2e": {"value": v, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import torch
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    from kronmult_gb300 import DeviceBatch, _lib
+
+    lib = _lib.lib()
+    b = make_batch(args.config, rank)
+    tdt = torch.float64 if args.dtype == "f64" else torch.float32
+    esize = 8 if args.dtype == "f64" else 4
+    db = DeviceBatch.from_host(b, device=dev, dtype=tdt)
+    stream = torch.cuda.Stream(dev)
+    flops_step = b.flops()
+    bytes_step = b.bytes(in_size=esize, out_size=esize)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            db.forward(stream=stream)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        db.forward(stream=stream)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = t.item()
+    per_launch_s = ms / 1e3 / args.steps
+    value = flops_step * world / per_launch_s / 1e9
+
+    # ---- end to end through the public API with pinned host buffers
+    h_in = torch.from_numpy(b.inputs).to(tdt).pin_memory()
+    h_fac = torch.from_numpy(b.factors).to(tdt).pin_memory()
+    h_out = torch.empty(db.outputs.shape, dtype=tdt).pin_memory()
+    h2d = h_in.numel() * esize + h_fac.numel() * esize
+    d2h = h_out.numel() * esize
+
+    def e2e_step():
+        db.inputs.copy_(h_in, non_blocking=True)
+        db.factors.copy_(h_fac, non_blocking=True)
+        db.forward(stream=stream)
+        h_out.copy_(db.outputs, non_blocking=True)
+
+    with torch.cuda.stream(stream):
+        e2e_step()
+        torch.cuda.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        ee0 = torch.cuda.Event(enable_timing=True)
+        ee1 = torch.cuda.Event(enable_timing=True)
+        ee0.record(stream)
+        for _ in range(args.e2e_steps):
+            e2e_step()
+        ee1.record(stream)
+        stream.synchronize()
+    e2e_ms = max(ee0.elapsed_time(ee1), (time.perf_counter() - t0) * 1e3) / args.e2e_steps
+    e2e_value = flops_step * world / (e2e_ms / 1e3) / 1e9
+
+    # ---- live roofline denominators
+    fp64_peak = None
+    if args.dtype == "f64":
+        import ctypes
+
+        g = ctypes.c_double(0)
+        if lib.kronmult_diag_fp64_fma_gflops(ctypes.byref(g)) == 0:
+            fp64_peak = g.value
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    hbm_src = "of measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks else "of fallback"
+    achieved_gbs = bytes_step / per_launch_s / 1e9
+    achieved_gflops = flops_step / per_launch_s / 1e9
+    traffic = None
+    try:
+        tr = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
+        traffic = tr.get(f"{args.config}_{args.dtype}")
+    except (OSError, ValueError):
+        pass
+    if args.dtype == "f64" and fp64_peak:
+        roofline = {"bound": "fp64", "achieved": achieved_gflops, "peak": fp64_peak, "unit": "GFLOP/s",
+                    "frac": achieved_gflops / fp64_peak, "traffic": traffic,
+                    "peak_source": "of measured (FP64 FMA probe kernel run by this benchmark)",
+                    "hbm": {"achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                            "frac": achieved_gbs / hbm_peak, "peak_source": hbm_src}}
+    else:
+        roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                    "frac": achieved_gbs / hbm_peak, "traffic": traffic, "peak_source": hbm_src}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(b, np.float64 if args.dtype == "f64" else np.float32)
+
+    if rank == 0:
+        _, wname = CONFIGS[args.config]
+        line = {
+            "metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": args.dtype,
+            "data": "synthetic (seeded PCG64; factors U[-1,1], inputs N(0,1))",
+            "config": {"workload": wname, "d": b.d, "n": b.n, "matrix_stride": b.stride, "nb_batch": b.nb,
+                       "outputs": b.n_out, "fan_in": b.nb // max(b.n_out, 1),
+                       "l2": "inputs (%.2f GB) larger than L2; no flush" % (b.inputs.nbytes / 1e9),
+                       "parallelism": f"output-group shards x{world}"},
+            "gbytes_per_s": achieved_gbs,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "GFLOP/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms},
+            "gpu_launches": args.steps,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

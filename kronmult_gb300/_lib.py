@@ -1,0 +1,92 @@
+"""ctypes binding of libkronmult_gb300.so (C ABI: include/kronmult_gb300.h).
+
+The library is the product: there is no CPU fallback.  If the shared library
+has not been built, loading raises instead of silently computing elsewhere.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libkronmult_gb300.so")
+
+KRONMULT_COMPUTE_FP32 = 0
+KRONMULT_COMPUTE_TF32 = 1
+KRONMULT_COMPUTE_BF16 = 2
+
+
+class Tuning(ctypes.Structure):
+    """Mirror of `kronmult_tuning`: launch-shape override, zero = heuristic."""
+
+    _fields_ = [("team_size", ctypes.c_int), ("ctas_per_sm", ctypes.c_int), ("entries_per_team", ctypes.c_int)]
+
+
+class KronmultError(RuntimeError):
+    """A non-zero status (a cudaError_t value) returned by the library."""
+
+    def __init__(self, status: int, where: str):
+        self.status = status
+        super().__init__(f"{where} failed with status {status}: {error_string(status)}")
+
+
+_lock = threading.Lock()
+_lib = None
+
+_vp = ctypes.c_void_p
+_i = ctypes.c_int
+_TP = ctypes.POINTER(Tuning)
+
+# (name, restype, argtypes); every symbol include/kronmult_gb300.h declares
+SIGNATURES = {
+    "kronmult_batched_f64": (_i, [_i, _i, _vp, _i, _vp, _vp, _vp, _i]),
+    "kronmult_batched_f32": (_i, [_i, _i, _vp, _i, _vp, _vp, _vp, _i]),
+    "kronmult_batched_f64_async": (_i, [_i, _i, _vp, _i, _vp, _vp, _vp, _i, _vp, _TP]),
+    "kronmult_batched_f32_async": (_i, [_i, _i, _vp, _i, _vp, _vp, _vp, _i, _vp, _TP]),
+    "kronmult_batched_f32_f64out_async": (_i, [_i, _i, _vp, _i, _vp, _vp, _vp, _i, _i, _vp, _TP]),
+    "kronmult_diag_fp64_fma_gflops": (_i, [ctypes.POINTER(ctypes.c_double)]),
+    "kronmult_pow_int": (ctypes.c_longlong, [_i, _i]),
+    "kronmult_error_string": (ctypes.c_char_p, [_i]),
+    "kronmult_abi_version": (_i, []),
+}
+
+
+def lib() -> ctypes.CDLL:
+    """Load the library once; raise if it is missing (build it with __graft_entry__.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise RuntimeError(
+                    f"{LIB_PATH} is missing: build the CUDA library first "
+                    "(python -c 'import __graft_entry__ as g; g.build()')")
+            h = ctypes.CDLL(LIB_PATH)
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(h, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = h
+    return _lib
+
+
+def error_string(status: int) -> str:
+    try:
+        s = lib().kronmult_error_string(int(status))
+        return s.decode() if s else "unknown"
+    except Exception:  # pragma: no cover - only used while formatting another error
+        return "unknown"
+
+
+def check(status: int, where: str) -> None:
+    if status != 0:
+        raise KronmultError(status, where)
+
+
+def tuning_ptr(t: Tuning | dict | None):
+    if t is None:
+        return None
+    if isinstance(t, dict):
+        t = Tuning(int(t.get("team_size", 0)), int(t.get("ctas_per_sm", 0)), int(t.get("entries_per_team", 0)))
+    return ctypes.byref(t)

@@ -1,0 +1,149 @@
+"""Python host mirror of the reference's `kronmult_batched` interface.
+
+`kronmult_batched(...)` has the reference's argument list and meaning
+(kronmult_gpu/kronmult.cuh:28-32): device-resident pointer arrays for the
+factors, inputs, outputs and workspaces, and it adds kron(A_k) . x_k into
+output k for every entry.  It is synchronous and raises `KronmultError` where the
+reference would return a failing cudaError.  Pointer arrays may be given as
+int64 CUDA tensors of device addresses or as raw device addresses (ints).
+
+`DeviceBatch` owns a structured batch in device memory (dense factor, input and
+output tensors plus index maps) and builds the pointer arrays from it; it is
+how the tests, the benchmark and the autograd wrapper drive the C ABI.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .workloads import Batch
+
+_FN = {torch.float64: "kronmult_batched_f64", torch.float32: "kronmult_batched_f32"}
+
+
+def _addr(x) -> int | None:
+    if x is None:
+        return None
+    if isinstance(x, torch.Tensor):
+        if x.numel() > 0 and not x.is_cuda:
+            raise ValueError("pointer arrays must be device-resident (CUDA tensors)")
+        return x.data_ptr()
+    return int(x)
+
+
+def _stream_handle(stream) -> int | None:
+    if stream is None:
+        return torch.cuda.current_stream().cuda_stream
+    if isinstance(stream, torch.cuda.Stream):
+        return stream.cuda_stream
+    return int(stream)
+
+
+def kronmult_batched(matrix_count: int, matrix_size: int, matrix_list_batched, matrix_stride: int,
+                     input_batched, output_batched, workspace_batched, nb_batch: int,
+                     dtype: torch.dtype = torch.float64) -> None:
+    """Mirror of kronmult_batched<T>: synchronous, reference semantics (see module doc)."""
+    if dtype not in _FN:
+        raise TypeError("kronmult_batched is defined for float64 and float32 only")
+    fn = getattr(_lib.lib(), _FN[dtype])
+    st = fn(int(matrix_count), int(matrix_size), _addr(matrix_list_batched), int(matrix_stride),
+            _addr(input_batched), _addr(output_batched), _addr(workspace_batched), int(nb_batch))
+    _lib.check(st, _FN[dtype])
+
+
+def kronmult_batched_async(matrix_count: int, matrix_size: int, matrix_list_batched, matrix_stride: int,
+                           input_batched, output_batched, workspace_batched, nb_batch: int,
+                           dtype: torch.dtype = torch.float64, stream=None, tuning=None) -> None:
+    """Enqueue the forward on `stream` (default: torch's current stream); no synchronisation."""
+    if dtype not in _FN:
+        raise TypeError("kronmult_batched is defined for float64 and float32 only")
+    name = _FN[dtype] + "_async"
+    fn = getattr(_lib.lib(), name)
+    st = fn(int(matrix_count), int(matrix_size), _addr(matrix_list_batched), int(matrix_stride),
+            _addr(input_batched), _addr(output_batched), _addr(workspace_batched), int(nb_batch),
+            _stream_handle(stream), _lib.tuning_ptr(tuning))
+    _lib.check(st, name)
+
+
+class DeviceBatch:
+    """A batch in device memory with the pointer arrays the C ABI consumes.
+
+    factors   (S*d, block)   row s*d+i holds factor i of set s (col-major, ld = stride)
+    inputs    (B, N)
+    outputs   (E, N)         accumulated into
+    fac_index, out_index     (B,) int64 maps entry -> factor set / output vector
+    """
+
+    def __init__(self, d: int, n: int, stride: int, factors: torch.Tensor, inputs: torch.Tensor,
+                 outputs: torch.Tensor, fac_index: torch.Tensor, out_index: torch.Tensor,
+                 with_workspace: bool = False):
+        self.d, self.n, self.stride = int(d), int(n), int(stride)
+        self.factors, self.inputs, self.outputs = factors, inputs, outputs
+        self.fac_index = fac_index.to(device=inputs.device, dtype=torch.int64)
+        self.out_index = out_index.to(device=inputs.device, dtype=torch.int64)
+        self.workspace = torch.empty_like(inputs) if with_workspace else None
+        self.build_pointers()
+
+    @classmethod
+    def from_host(cls, b: Batch, device="cuda", dtype=torch.float64, out_dtype=None,
+                  with_workspace: bool = False) -> "DeviceBatch":
+        out_dtype = out_dtype or dtype
+        t = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a)).to(device=device, dtype=dt)
+        return cls(b.d, b.n, b.stride, t(b.factors, dtype), t(b.inputs, dtype), t(b.out_init, out_dtype),
+                   torch.from_numpy(b.fac_index), torch.from_numpy(b.out_index), with_workspace)
+
+    @property
+    def nb(self) -> int:
+        return int(self.inputs.shape[0])
+
+    @property
+    def N(self) -> int:
+        return self.n ** self.d
+
+    def build_pointers(self) -> None:
+        """(Re)build the device pointer arrays from the current tensors."""
+        dev = self.inputs.device
+        fes = self.factors.element_size()
+        ies = self.inputs.element_size()
+        oes = self.outputs.element_size()
+        blk = self.factors.shape[1] if self.factors.dim() == 2 else 0
+        B, d = self.nb, self.d
+        i = torch.arange(d, device=dev, dtype=torch.int64)
+        self.mat_ptrs = (self.factors.data_ptr()
+                         + ((self.fac_index[:, None] * d + i[None, :]) * (blk * fes))).reshape(-1).contiguous()
+        k = torch.arange(B, device=dev, dtype=torch.int64)
+        self.in_ptrs = (self.inputs.data_ptr() + k * (self.inputs.shape[1] * ies)).contiguous()
+        self.out_ptrs = (self.outputs.data_ptr() + self.out_index * (self.outputs.shape[1] * oes)).contiguous()
+        self.ws_ptrs = None
+        if self.workspace is not None:
+            self.ws_ptrs = (self.workspace.data_ptr() + k * (self.workspace.shape[1] * ies)).contiguous()
+
+    def forward(self, stream=None, tuning=None, sync: bool = False) -> None:
+        """outputs[out_index[k]] += kron(factors of set fac_index[k]) . inputs[k] for all k."""
+        dt = self.inputs.dtype
+        if self.outputs.dtype == dt:
+            if sync:
+                kronmult_batched(self.d, self.n, self.mat_ptrs, self.stride, self.in_ptrs, self.out_ptrs,
+                                 self.ws_ptrs, self.nb, dtype=dt)
+            else:
+                kronmult_batched_async(self.d, self.n, self.mat_ptrs, self.stride, self.in_ptrs, self.out_ptrs,
+                                       self.ws_ptrs, self.nb, dtype=dt, stream=stream, tuning=tuning)
+        elif dt == torch.float32 and self.outputs.dtype == torch.float64:
+            forward_f32_f64out(self, compute=_lib.KRONMULT_COMPUTE_FP32, stream=stream, tuning=tuning)
+            if sync:
+                torch.cuda.synchronize()
+        else:
+            raise TypeError(f"unsupported storage/output dtypes {dt}/{self.outputs.dtype}")
+
+
+def forward_f32_f64out(b: DeviceBatch, compute: int = _lib.KRONMULT_COMPUTE_FP32, stream=None,
+                       tuning=None) -> None:
+    """FP32 factors/inputs, FP32 (or TF32/BF16 tensor-core) contraction, FP64 output accumulation."""
+    fn = _lib.lib().kronmult_batched_f32_f64out_async
+    st = fn(b.d, b.n, b.mat_ptrs.data_ptr(), b.stride, b.in_ptrs.data_ptr(), b.out_ptrs.data_ptr(),
+            None if b.ws_ptrs is None else b.ws_ptrs.data_ptr(), b.nb, int(compute), _stream_handle(stream),
+            _lib.tuning_ptr(tuning))
+    _lib.check(st, "kronmult_batched_f32_f64out_async")

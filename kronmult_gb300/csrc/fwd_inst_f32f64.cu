@@ -1,0 +1,3 @@
+// Explicit instantiation of the forward kernels for (storage, output) = (float,double).
+#include "fwd_kernels.cuh"
+KGB_FWD_INSTANTIATE(float, double)

@@ -1,0 +1,3 @@
+// Explicit instantiation of the forward kernels for (storage, output) = (double,double).
+#include "fwd_kernels.cuh"
+KGB_FWD_INSTANTIATE(double, double)

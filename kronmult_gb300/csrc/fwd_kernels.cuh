@@ -1,0 +1,303 @@
+// Forward kernels: output[k] += kron(A_{k,0..d-1}) . input[k].
+//
+// Replaces the reference's one-CTA-per-entry kernel that ping-pongs through the
+// caller's global `input`/`workspace` vectors (kronmult_gpu/kronmult.cu:95-167).
+// Here each entry's N-vector and its d factors are staged in shared memory once,
+// the d mode products of the backward Algorithm-993 sweep run in place in that
+// buffer through registers, and consecutive entries that target the same output
+// vector are summed in registers before one atomic add per element.
+//
+// Mode product (kronmult_gpu/kronmult.cu:54-78): with X the current vector seen
+// as an n x F col-major matrix (F = N/n fibres of n contiguous values),
+//     Y[c + r*F] = sum_{k=0..n-1} A_i(r, k) * X[k + c*n]
+// summed k-ascending from 0 with fused multiply-adds, exactly as the reference
+// kernel's `dotprod += X * Mt` does.  Modes run i = d-1 .. 0; after d steps the
+// index rotation returns the vector to its natural order.
+#pragma once
+#include "common.cuh"
+
+namespace kgb {
+
+template <typename T, typename TO> struct FwdArgs {
+    const T *const *mats;  // nb*d factor pointers, entry k's factors at [k*d, k*d+d)
+    const T *const *in;    // nb input pointers (N values each)
+    TO *const *out;        // nb output pointers (may alias)
+    T *const *ws;          // nb workspace pointers (generic global path only; may be null)
+    long long nb;          // number of entries
+    int d, n, stride;      // factor count, factor size, factor leading dimension
+    int N;                 // n^d
+    int team_size;         // threads per team
+    int teams_per_cta;     // teams in one CTA
+    int entries_per_team;  // contiguous entries each team processes
+    int team_elems;        // shared-memory elements reserved per team
+    int vec_pad;           // offset of the factor area inside a team's slice (elements)
+};
+
+// ---- helpers ---------------------------------------------------------------
+
+// copy N values of an input vector into shared memory, 16-byte vectors when the
+// source is 16-byte aligned and N*sizeof(T) is a multiple of 16
+template <typename T>
+__device__ __forceinline__ void stage_vector(T *dst, const T *src, int N, const Team &tm)
+{
+    const size_t bytes = (size_t)N * sizeof(T);
+    if (((reinterpret_cast<uintptr_t>(src) & 15u) == 0) && ((bytes & 15u) == 0)) {
+        const int nv = (int)(bytes >> 4);
+        int4 *d4 = reinterpret_cast<int4 *>(dst);
+        const int4 *s4 = reinterpret_cast<const int4 *>(src);
+        for (int v = tm.rank; v < nv; v += tm.size) d4[v] = __ldcs(s4 + v);
+    } else {
+        for (int v = tm.rank; v < N; v += tm.size) dst[v] = __ldcs(src + v);
+    }
+}
+
+// copy the d factors of an entry into shared memory as fac[i*n*n + r + k*n] = A_i(r,k)
+template <typename T, int NN>
+__device__ __forceinline__ void stage_factors(T *fac, const T *const *mats, int d, int stride, const Team &tm)
+{
+    constexpr int NN2 = NN * NN;
+    for (int idx = tm.rank; idx < d * NN2; idx += tm.size) {
+        const int i = idx / NN2;
+        const int rem = idx - i * NN2;
+        const int k = rem / NN;
+        const int r = rem - k * NN;
+        fac[idx] = mats[i][r + (size_t)k * stride];
+    }
+}
+
+// bytes of the widest aligned vector load for one fibre of NN values of type T
+template <typename T, int NN> struct FibreVec {
+    static constexpr int bytes = NN * (int)sizeof(T);
+    static constexpr int width = (bytes % 16 == 0) ? 16 : (bytes % 8 == 0) ? 8 : (int)sizeof(T);
+};
+
+template <typename T, int NN> __device__ __forceinline__ void load_fibre(const T *p, T (&x)[NN])
+{
+    constexpr int W = FibreVec<T, NN>::width;
+    if constexpr (W == 16) {
+        const int4 *p4 = reinterpret_cast<const int4 *>(p);
+#pragma unroll
+        for (int v = 0; v < (int)(NN * sizeof(T) / 16); ++v) {
+            int4 t = p4[v];
+            *reinterpret_cast<int4 *>(&x[v * 16 / sizeof(T)]) = t;
+        }
+    } else if constexpr (W == 8 && sizeof(T) == 4) {
+        const float2 *p2 = reinterpret_cast<const float2 *>(p);
+#pragma unroll
+        for (int v = 0; v < NN / 2; ++v) {
+            float2 t = p2[v];
+            x[2 * v] = t.x;
+            x[2 * v + 1] = t.y;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < NN; ++k) x[k] = p[k];
+    }
+}
+
+template <typename T> __device__ __forceinline__ T fma_t(T a, T b, T c) { return fma(a, b, c); }
+template <> __device__ __forceinline__ float fma_t<float>(float a, float b, float c) { return fmaf(a, b, c); }
+
+// ---- shared-memory, register in-place kernel (compile-time n) -------------
+//
+// Thread `rank` of a team owns fibres c = rank + q*team_size (q < QMAX) in every
+// mode and computes all n outputs of each of its fibres, so each staged input
+// value is read from shared memory once per mode.  The mode is done in place:
+// every thread reads its fibres into registers, the team synchronises, and the
+// results are written to their rotated positions c + r*F.
+template <typename T, typename TO, int NN, int QMAX>
+__global__ void __launch_bounds__(512) fwd_smem_kernel(const FwdArgs<T, TO> a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const Team tm(a.team_size);
+    T *buf = reinterpret_cast<T *>(smem_raw) + (size_t)tm.id * a.team_elems;
+    T *fac = buf + a.vec_pad;
+    const int N = a.N;
+    const int F = N / NN;
+    const int d = a.d;
+
+    const long long team_global = (long long)blockIdx.x * a.teams_per_cta + tm.id;
+    long long e = team_global * a.entries_per_team;
+    const long long e_end = min(e + (long long)a.entries_per_team, a.nb);
+
+    TO acc[QMAX][NN];
+    TO *cur = nullptr;
+
+    for (; e < e_end; ++e) {
+        const T *x = a.in[e];
+        TO *o = a.out[e];
+        stage_vector(buf, x, N, tm);
+        stage_factors<T, NN>(fac, a.mats + e * d, d, a.stride, tm);
+        tm.sync();
+
+        T y[QMAX][NN];
+        for (int i = d - 1; i >= 0; --i) {
+            const T *M = fac + i * NN * NN;
+            // small factors are held in registers; larger ones are read from shared
+            // memory, where every lane of a warp reads the same address (broadcast)
+            constexpr bool kRegM = NN * NN * sizeof(T) <= 128;
+            T m[kRegM ? NN * NN : 1];
+            if constexpr (kRegM) {
+#pragma unroll
+                for (int j = 0; j < NN * NN; ++j) m[j] = M[j];
+            }
+#pragma unroll
+            for (int q = 0; q < QMAX; ++q) {
+                const int c = tm.rank + q * tm.size;
+                if (c < F) {
+                    T xv[NN];
+                    load_fibre<T, NN>(buf + c * NN, xv);
+#pragma unroll
+                    for (int r = 0; r < NN; ++r) {
+                        T s = T(0);
+#pragma unroll
+                        for (int k = 0; k < NN; ++k) {
+                            const T mv = kRegM ? m[kRegM ? r + k * NN : 0] : M[r + k * NN];
+                            s = fma_t<T>(mv, xv[k], s);
+                        }
+                        y[q][r] = s;
+                    }
+                }
+            }
+            tm.sync();  // every read of buf (and fac) for this mode is done
+            if (i > 0) {
+#pragma unroll
+                for (int q = 0; q < QMAX; ++q) {
+                    const int c = tm.rank + q * tm.size;
+                    if (c < F) {
+#pragma unroll
+                        for (int r = 0; r < NN; ++r) buf[c + r * F] = y[q][r];
+                    }
+                }
+                tm.sync();
+            }
+        }
+        // y[q][r] is element c + r*F of kron(A) . x
+        if (o != cur) {
+            if (cur != nullptr) {
+#pragma unroll
+                for (int q = 0; q < QMAX; ++q) {
+                    const int c = tm.rank + q * tm.size;
+                    if (c < F) {
+#pragma unroll
+                        for (int r = 0; r < NN; ++r) atomic_add<TO>(cur + c + r * F, acc[q][r]);
+                    }
+                }
+            }
+            cur = o;
+#pragma unroll
+            for (int q = 0; q < QMAX; ++q)
+#pragma unroll
+                for (int r = 0; r < NN; ++r) acc[q][r] = (TO)y[q][r];
+        } else {
+#pragma unroll
+            for (int q = 0; q < QMAX; ++q)
+#pragma unroll
+                for (int r = 0; r < NN; ++r) acc[q][r] += (TO)y[q][r];
+        }
+    }
+    if (cur != nullptr) {
+#pragma unroll
+        for (int q = 0; q < QMAX; ++q) {
+            const int c = tm.rank + q * tm.size;
+            if (c < F) {
+#pragma unroll
+                for (int r = 0; r < NN; ++r) atomic_add<TO>(cur + c + r * F, acc[q][r]);
+            }
+        }
+    }
+}
+
+// ---- generic kernel (runtime n, any N) ------------------------------------
+//
+// One CTA per entry (grid-stride over entries), one thread per output element.
+// Uses two shared-memory buffers when 2N values fit; otherwise it ping-pongs
+// through the caller's `input` and `workspace` vectors in global memory, which it
+// then clobbers, as the reference does (kronmult_gpu/kronmult.cu:119-121).
+template <typename T, typename TO>
+__global__ void __launch_bounds__(256) fwd_generic_kernel(const FwdArgs<T, TO> a, int use_smem)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int N = a.N, n = a.n, d = a.d;
+    const int F = (n > 0) ? N / n : 0;
+    T *fac = reinterpret_cast<T *>(smem_raw);  // n*n, transposed-free copy of the current factor
+    T *s0 = fac + ((n * n + 1) & ~1);
+    T *s1 = s0 + ((N + 1) & ~1);
+    for (long long e = blockIdx.x; e < a.nb; e += gridDim.x) {
+        const T *x = a.in[e];
+        TO *o = a.out[e];
+        T *src, *dst;
+        if (use_smem) {
+            for (int v = threadIdx.x; v < N; v += blockDim.x) s0[v] = x[v];
+            src = s0;
+            dst = s1;
+        } else {
+            src = const_cast<T *>(x);
+            dst = a.ws[e];
+        }
+        __syncthreads();
+        for (int i = d - 1; i >= 0; --i) {
+            const T *A = a.mats[e * d + i];
+            for (int v = threadIdx.x; v < n * n; v += blockDim.x) {
+                const int k = v / n, r = v - k * n;
+                fac[v] = A[r + (size_t)k * a.stride];
+            }
+            __syncthreads();
+            for (int p = threadIdx.x; p < N; p += blockDim.x) {
+                const int r = p / F, c = p - r * F;
+                T s = T(0);
+                for (int k = 0; k < n; ++k) s = fma_t<T>(fac[r + k * n], src[k + (size_t)c * n], s);
+                dst[p] = s;
+            }
+            __syncthreads();
+            T *t = src;
+            src = dst;
+            dst = t;
+        }
+        for (int p = threadIdx.x; p < N; p += blockDim.x) atomic_add<TO>(o + p, (TO)src[p]);
+        __syncthreads();
+    }
+}
+
+// kernel pointer lookup, defined once per (T, TO) instantiation unit
+template <typename T, typename TO> using FwdSmemFn = void (*)(const FwdArgs<T, TO>);
+template <typename T, typename TO> FwdSmemFn<T, TO> fwd_smem_lookup(int nn, int qmax);
+template <typename T, typename TO> void *fwd_generic_ptr();
+
+}  // namespace kgb
+
+// explicit instantiation of the forward kernels for one (T, TO) pair
+#define KGB_FWD_INSTANTIATE(T, TO)                                                                     \
+    namespace kgb {                                                                                    \
+    template <> FwdSmemFn<T, TO> fwd_smem_lookup<T, TO>(int nn, int qmax)                             \
+    {                                                                                                  \
+        switch (nn * 16 + qmax) {                                                                      \
+        case 2 * 16 + 1: return fwd_smem_kernel<T, TO, 2, 1>;                                          \
+        case 2 * 16 + 2: return fwd_smem_kernel<T, TO, 2, 2>;                                          \
+        case 2 * 16 + 4: return fwd_smem_kernel<T, TO, 2, 4>;                                          \
+        case 2 * 16 + 8: return fwd_smem_kernel<T, TO, 2, 8>;                                          \
+        case 3 * 16 + 1: return fwd_smem_kernel<T, TO, 3, 1>;                                          \
+        case 3 * 16 + 2: return fwd_smem_kernel<T, TO, 3, 2>;                                          \
+        case 3 * 16 + 4: return fwd_smem_kernel<T, TO, 3, 4>;                                          \
+        case 3 * 16 + 8: return fwd_smem_kernel<T, TO, 3, 8>;                                          \
+        case 4 * 16 + 1: return fwd_smem_kernel<T, TO, 4, 1>;                                          \
+        case 4 * 16 + 2: return fwd_smem_kernel<T, TO, 4, 2>;                                          \
+        case 4 * 16 + 4: return fwd_smem_kernel<T, TO, 4, 4>;                                          \
+        case 4 * 16 + 8: return fwd_smem_kernel<T, TO, 4, 8>;                                          \
+        case 5 * 16 + 1: return fwd_smem_kernel<T, TO, 5, 1>;                                          \
+        case 5 * 16 + 2: return fwd_smem_kernel<T, TO, 5, 2>;                                          \
+        case 5 * 16 + 4: return fwd_smem_kernel<T, TO, 5, 4>;                                          \
+        case 6 * 16 + 1: return fwd_smem_kernel<T, TO, 6, 1>;                                          \
+        case 6 * 16 + 2: return fwd_smem_kernel<T, TO, 6, 2>;                                          \
+        case 6 * 16 + 4: return fwd_smem_kernel<T, TO, 6, 4>;                                          \
+        case 7 * 16 + 1: return fwd_smem_kernel<T, TO, 7, 1>;                                          \
+        case 7 * 16 + 2: return fwd_smem_kernel<T, TO, 7, 2>;                                          \
+        case 7 * 16 + 4: return fwd_smem_kernel<T, TO, 7, 4>;                                          \
+        case 8 * 16 + 1: return fwd_smem_kernel<T, TO, 8, 1>;                                          \
+        case 8 * 16 + 2: return fwd_smem_kernel<T, TO, 8, 2>;                                          \
+        case 8 * 16 + 4: return fwd_smem_kernel<T, TO, 8, 4>;                                          \
+        default: return nullptr;                                                                       \
+        }                                                                                              \
+    }                                                                                                  \
+    template <> void *fwd_generic_ptr<T, TO>() { return (void *)fwd_generic_kernel<T, TO>; }          \
+    }

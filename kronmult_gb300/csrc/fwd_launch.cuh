@@ -1,0 +1,187 @@
+// Host-side launch planning for the forward kernels.
+#pragma once
+#include <climits>
+#include <cstdint>
+#include <mutex>
+#include "fwd_kernels.cuh"
+#include "kronmult_gb300.h"
+
+namespace kgb {
+
+// per-device properties, queried once
+struct DeviceInfo {
+    int sms = 0;
+    int max_smem_optin = 0;  // bytes of dynamic shared memory one CTA may opt into
+};
+
+const DeviceInfo &device_info(int dev);
+
+// remembers which kernels have had their dynamic shared-memory limit raised
+bool ensure_smem_attr(const void *fn, size_t smem);
+
+// resident CTAs per SM for a kernel/launch shape (cached)
+int occupancy(const void *fn, int block, size_t smem);
+
+inline long long pow_ll(int b, int e)
+{
+    long long r = 1;
+    for (int i = 0; i < e; ++i) {
+        r *= b;
+        if (r > (long long)INT_MAX) return (long long)INT_MAX + 1;
+    }
+    return r;
+}
+
+inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
+
+// largest power of two <= v (v >= 1)
+inline int pow2_floor(long long v)
+{
+    int p = 1;
+    while ((long long)p * 2 <= v) p *= 2;
+    return p;
+}
+
+// A resolved forward launch.
+template <typename T, typename TO> struct FwdPlan {
+    FwdArgs<T, TO> args{};
+    const void *fn = nullptr;
+    bool smem_path = false;  // register in-place shared-memory kernel
+    int use_smem = 0;        // generic kernel: shared-memory ping-pong
+    dim3 grid, block;
+    size_t smem = 0;
+};
+
+// Checks arguments and fills a plan.  Returns cudaSuccess, cudaErrorInvalidValue,
+// or cudaErrorNotSupported (vector too long for any path without a workspace).
+template <typename T, typename TO>
+int plan_forward(FwdPlan<T, TO> &pl, int d, int n, const T *const *mats, int stride, const T *const *in,
+                 TO *const *out, T *const *ws, long long nb, const kronmult_tuning *tune)
+{
+    if (d < 0 || n < 0 || nb < 0) return cudaErrorInvalidValue;
+    if (stride < (n > 0 ? n : 1)) return cudaErrorInvalidValue;
+    const long long Nl = pow_ll(n, d);
+    if (Nl > (long long)INT_MAX) return cudaErrorInvalidValue;
+    pl.args = FwdArgs<T, TO>{};
+    pl.fn = nullptr;
+    if (nb == 0 || n == 0) return cudaSuccess;  // nothing to add
+    if (!in || !out || (d > 0 && !mats)) return cudaErrorInvalidValue;
+
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return cudaErrorInvalidDevice;
+    const DeviceInfo &di = device_info(dev);
+    const int N = (int)Nl;
+
+    FwdArgs<T, TO> &a = pl.args;
+    a.mats = mats;
+    a.in = in;
+    a.out = out;
+    a.ws = ws;
+    a.nb = nb;
+    a.d = d;
+    a.n = n;
+    a.stride = stride;
+    a.N = N;
+
+    // ---- register in-place shared-memory path: 2 <= n <= 8, d >= 1
+    if (n >= 2 && n <= 8 && d >= 1) {
+        const int F = N / n;
+        const int qcap = (n <= 4) ? 8 : 4;
+        int ts = 8;
+        if (tune && tune->team_size > 0) {
+            ts = tune->team_size;
+        } else {
+            // smallest team that leaves every thread at most ~2-4 fibres
+            const int qtarget = (n <= 4) ? 4 : 2;
+            while (ts < 512 && (long long)ts * qtarget < F) ts *= 2;
+        }
+        const int q = (F + ts - 1) / ts;
+        int qmax = 1;
+        while (qmax < q) qmax *= 2;
+        const bool ts_ok = (ts == 8 || ts == 16 || ts == 32 || ts == 64 || ts == 128 || ts == 256 || ts == 512);
+        if (ts_ok && qmax <= qcap) {
+            const int vpad = round_up(N, 16 / (int)sizeof(T));
+            const int team_elems = vpad + round_up(d * n * n, 16 / (int)sizeof(T));
+            const size_t team_bytes = (size_t)team_elems * sizeof(T);
+            int block = ts >= 256 ? ts : 256;
+            int teams = block / ts;
+            // named barriers 1..15 limit the number of multi-warp teams per CTA
+            while (ts >= 64 && ts < block && teams > 15) {
+                block /= 2;
+                teams = block / ts;
+            }
+            while (teams > 1 && (size_t)teams * team_bytes > (size_t)di.max_smem_optin) {
+                block /= 2;
+                teams = block / ts;
+            }
+            if (block < 32) block = 32, teams = block / ts;
+            const size_t smem = (size_t)teams * team_bytes;
+            if (smem <= (size_t)di.max_smem_optin) {
+                auto fn = fwd_smem_lookup<T, TO>(n, qmax);
+                if (fn && ensure_smem_attr((const void *)fn, smem)) {
+                    int per_sm = (tune && tune->ctas_per_sm > 0) ? tune->ctas_per_sm
+                                                                 : occupancy((const void *)fn, block, smem);
+                    if (per_sm < 1) per_sm = 1;
+                    const long long total_teams = (long long)di.sms * per_sm * teams;
+                    long long ept = (tune && tune->entries_per_team > 0) ? tune->entries_per_team
+                                                                         : (nb + total_teams - 1) / total_teams;
+                    if (ept < 1) ept = 1;
+                    if (ept > INT_MAX) ept = INT_MAX;
+                    const long long per_cta = ept * teams;
+                    const long long grid = (nb + per_cta - 1) / per_cta;
+                    if (grid <= INT_MAX) {
+                        a.team_size = ts;
+                        a.teams_per_cta = teams;
+                        a.entries_per_team = (int)ept;
+                        a.team_elems = team_elems;
+                        a.vec_pad = vpad;
+                        pl.fn = (const void *)fn;
+                        pl.smem_path = true;
+                        pl.grid = dim3((unsigned)grid);
+                        pl.block = dim3((unsigned)block);
+                        pl.smem = smem;
+                        return cudaSuccess;
+                    }
+                }
+            }
+        }
+    }
+
+    // ---- generic path
+    const void *fn = fwd_generic_ptr<T, TO>();
+    const size_t smem_s = ((size_t)round_up(n * n, 2) + 2 * (size_t)round_up(N, 2)) * sizeof(T);
+    if (smem_s <= (size_t)di.max_smem_optin && ensure_smem_attr(fn, smem_s)) {
+        pl.use_smem = 1;
+        pl.smem = smem_s;
+    } else {
+        if (!ws) return cudaErrorNotSupported;
+        pl.use_smem = 0;
+        pl.smem = (size_t)round_up(n * n, 2) * sizeof(T);
+        if (!ensure_smem_attr(fn, pl.smem)) return cudaErrorInvalidValue;
+    }
+    const int block = 256;
+    int per_sm = occupancy(fn, block, pl.smem);
+    if (per_sm < 1) per_sm = 1;
+    long long grid = (long long)di.sms * per_sm * 4;
+    if (grid > nb) grid = nb;
+    pl.fn = fn;
+    pl.smem_path = false;
+    pl.grid = dim3((unsigned)grid);
+    pl.block = dim3(block);
+    return cudaSuccess;
+}
+
+template <typename T, typename TO> int launch_plan(const FwdPlan<T, TO> &pl, cudaStream_t st)
+{
+    if (!pl.fn) return cudaSuccess;
+    if (pl.smem_path) {
+        auto fn = reinterpret_cast<void (*)(const FwdArgs<T, TO>)>(const_cast<void *>(pl.fn));
+        fn<<<pl.grid, pl.block, pl.smem, st>>>(pl.args);
+    } else {
+        auto fn = reinterpret_cast<void (*)(const FwdArgs<T, TO>, int)>(const_cast<void *>(pl.fn));
+        fn<<<pl.grid, pl.block, pl.smem, st>>>(pl.args, pl.use_smem);
+    }
+    return (int)cudaGetLastError();
+}
+
+}  // namespace kgb

@@ -1,0 +1,93 @@
+"""The C ABI library: it loads, exports every symbol include/*.h declares, and its
+host-side argument checks reject bad calls before touching a GPU.  No GPU needed."""
+import ctypes
+import glob
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+CUDA_ERROR_INVALID_VALUE = 1
+
+
+def declared_symbols():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(kronmult_\w+)\s*\(", text, flags=re.M):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from kronmult_gb300 import _build, _lib
+
+    if not os.path.exists(_lib.LIB_PATH):
+        _build.build()
+    return _lib.lib()
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    assert "kronmult_batched_f64" in names and "kronmult_batched_f32" in names
+
+
+def test_every_declared_symbol_is_exported(lib):
+    from kronmult_gb300 import _lib
+
+    for name in declared_symbols():
+        assert hasattr(lib, name), f"{name} declared in include/ but not exported"
+        assert name in _lib.SIGNATURES, f"{name} has no ctypes signature in kronmult_gb300/_lib.py"
+
+
+def test_pow_int_and_version(lib):
+    assert lib.kronmult_pow_int(4, 6) == 4096
+    assert lib.kronmult_pow_int(3, 0) == 1
+    assert lib.kronmult_pow_int(2, 40) > 2**31 - 1  # saturates above the int range
+    assert lib.kronmult_abi_version() >= 1
+
+
+@pytest.mark.parametrize("args", [
+    dict(d=-1, n=4, stride=4, nb=1),     # negative factor count
+    dict(d=2, n=-4, stride=4, nb=1),     # negative size
+    dict(d=2, n=4, stride=3, nb=1),      # stride below the matrix size
+    dict(d=2, n=4, stride=4, nb=-5),     # negative batch
+    dict(d=40, n=4, stride=4, nb=1),     # n^d beyond the 32-bit vector length
+])
+def test_invalid_arguments_rejected_on_host(lib, args):
+    dummy = ctypes.c_void_p(16)
+    for fn in (lib.kronmult_batched_f64_async, lib.kronmult_batched_f32_async):
+        rc = fn(args["d"], args["n"], dummy, args["stride"], dummy, dummy, dummy, args["nb"], None, None)
+        assert rc == CUDA_ERROR_INVALID_VALUE
+
+
+def test_null_tables_rejected(lib):
+    rc = lib.kronmult_batched_f64_async(2, 4, None, 4, None, None, None, 3, None, None)
+    assert rc == CUDA_ERROR_INVALID_VALUE
+
+
+def test_empty_batch_is_success_without_launch(lib):
+    assert lib.kronmult_batched_f64_async(3, 4, None, 4, None, None, None, 0, None, None) == 0
+    assert lib.kronmult_batched_f32_async(3, 0, None, 4, None, None, None, 7, None, None) == 0
+
+
+def test_error_string(lib):
+    from kronmult_gb300 import _lib
+
+    assert "invalid argument" in _lib.error_string(1).lower()
+
+
+def test_python_mirror_raises(lib):
+    import kronmult_gb300 as K
+
+    with pytest.raises(K.KronmultError) as e:
+        K.kronmult_batched(2, 4, 8, 3, 8, 8, None, 1)
+    assert e.value.status == CUDA_ERROR_INVALID_VALUE
+    with pytest.raises(TypeError):
+        import torch
+
+        K.kronmult_batched(2, 4, 8, 4, 8, 8, None, 1, dtype=torch.float16)

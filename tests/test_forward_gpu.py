@@ -1,0 +1,182 @@
+"""Parity of the CUDA forward with the reference's outputs (golden fixtures) and
+with the C oracle on seeded batches of every configuration's shape; full-size
+checks through size-independent properties.  Tolerances: relative L2 <= 1e-13
+for FP64 (atomic summation order is the only permitted difference), 1e-5 for
+FP32 against the FP64 result."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import golden_names, load_golden
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-13
+TOL32 = 1e-5
+
+
+def run(b, cuda, dtype=torch.float64, out_dtype=None, tuning=None, sync=False, ws=False):
+    from kronmult_gb300 import DeviceBatch
+
+    db = DeviceBatch.from_host(b, device=cuda, dtype=dtype, out_dtype=out_dtype, with_workspace=ws)
+    db.forward(tuning=tuning, sync=sync)
+    torch.cuda.synchronize()
+    return db.outputs.cpu().numpy(), db
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_golden_f64(cuda, name):
+    b, z = load_golden(name)
+    got, _ = run(b, cuda, sync=True)
+    assert O.rel_l2(got, z["expected_f64"]) <= TOL64
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_golden_f32(cuda, name):
+    b, z = load_golden(name)
+    got, _ = run(b, cuda, dtype=torch.float32, sync=True)
+    # FP32 against the reference's own FP32 result and against FP64
+    assert O.rel_l2(got, z["expected_f32"]) <= TOL32
+    assert O.rel_l2(got, z["expected_f64"]) <= TOL32
+
+
+def test_config1_full_f64(cuda):
+    from kronmult_gb300 import workloads as W
+
+    b = W.config1()
+    got, _ = run(b, cuda)
+    assert O.rel_l2(got, O.forward(b)) <= TOL64
+
+
+def test_config2_sample_f64(cuda):
+    from kronmult_gb300 import workloads as W
+
+    b = W.config2(scale=64 / 4096)
+    got, _ = run(b, cuda)
+    assert O.rel_l2(got, O.forward(b)) <= TOL64
+
+
+@pytest.mark.parametrize("gi", range(4))
+def test_config3_groups_f64(cuda, gi):
+    from kronmult_gb300 import workloads as W
+
+    b = W.config3(scale=0.02)[gi]
+    got, _ = run(b, cuda)
+    assert O.rel_l2(got, O.forward(b)) <= TOL64
+
+
+def test_config4_fp32_f64out(cuda):
+    from kronmult_gb300 import workloads as W
+
+    b = W.config4(scale=16 / 4096)
+    got, _ = run(b, cuda, dtype=torch.float32, out_dtype=torch.float64)
+    ref32 = O.forward(b, dtype=np.float32, out_dtype=np.float64)
+    ref64 = O.forward(b)
+    assert O.rel_l2(got, ref32) <= 1e-6
+    assert O.rel_l2(got, ref64) <= TOL32
+
+
+def test_config5_shared_factors(cuda):
+    from kronmult_gb300 import workloads as W
+
+    b = W.config5(scale=32 / 2048)
+    got, _ = run(b, cuda)
+    assert O.rel_l2(got, O.forward(b)) <= TOL64
+    got32, _ = run(b, cuda, dtype=torch.float32)
+    assert O.rel_l2(got32, O.forward(b)) <= TOL32
+
+
+@pytest.mark.parametrize("team_size", [8, 16, 32, 64, 128, 256, 512])
+def test_team_sizes_agree(cuda, team_size):
+    """Every launch shape the autotuner may pick gives the oracle's result."""
+    from kronmult_gb300 import workloads as W
+
+    b = W.make_batch(5, 4, 5, 7, 6, seed=99)
+    got, _ = run(b, cuda, tuning={"team_size": team_size, "entries_per_team": 3})
+    assert O.rel_l2(got, O.forward(b)) <= TOL64
+
+
+def test_inputs_not_modified(cuda):
+    from kronmult_gb300 import workloads as W
+
+    b = W.config1(scale=4 / 1024)
+    _, db = run(b, cuda)
+    assert np.array_equal(db.inputs.cpu().numpy(), b.inputs)
+
+
+def test_aliased_inputs(cuda):
+    """Several entries reading one input vector (the reference cannot do this, it
+    overwrites its inputs)."""
+    from kronmult_gb300 import DeviceBatch
+    from kronmult_gb300 import workloads as W
+
+    b = W.make_batch(3, 4, 4, 3, 4, seed=5)
+    db = DeviceBatch.from_host(b, device=cuda)
+    db.in_ptrs = torch.full_like(db.in_ptrs, db.inputs.data_ptr())
+    db.forward(sync=True)
+    b2 = W.Batch(b.name, b.d, b.n, b.stride, b.block, b.factors, np.repeat(b.inputs[:1], b.nb, 0), b.out_init,
+                 b.fac_index, b.out_index)
+    assert O.rel_l2(db.outputs.cpu().numpy(), O.forward(b2)) <= TOL64
+
+
+def test_large_vector_global_path(cuda):
+    """n^d beyond shared memory goes through input/workspace in global memory."""
+    from kronmult_gb300 import workloads as W
+
+    b = W.make_batch(5, 8, 8, 1, 2, seed=31)  # N = 32768 doubles = 256 KiB
+    ref = O.forward(b)
+    got, _ = run(b, cuda, ws=True)
+    assert O.rel_l2(got, ref) <= TOL64
+
+
+def test_reference_signature_mirror(cuda):
+    """The Python mirror of kronmult_batched<double> with raw device pointer arrays."""
+    import kronmult_gb300 as K
+    from kronmult_gb300 import workloads as W
+
+    b = W.config1(scale=8 / 1024)
+    db = K.DeviceBatch.from_host(b, device=cuda)
+    K.kronmult_batched(b.d, b.n, db.mat_ptrs, b.stride, db.in_ptrs, db.out_ptrs, None, b.nb)
+    assert O.rel_l2(db.outputs.cpu().numpy(), O.forward(b)) <= TOL64
+
+
+def test_full_config2_checksum(cuda):
+    """Full-size configuration 2 (36864 entries, N = 4096): the sum of every output
+    vector equals sum_k kron(colsum(A_k,0), ..., colsum(A_k,5)) . x_k, computed on the
+    host from the inputs alone."""
+    from kronmult_gb300 import workloads as W
+
+    b = W.config2()
+    got, db = run(b, cuda)
+    n, d = b.n, b.d
+    cs = np.empty((b.nb, d, n))
+    for i in range(d):
+        F = b.factors[b.fac_index * d + i][:, :b.stride * n].reshape(b.nb, n, b.stride)[:, :, :n]
+        cs[:, i, :] = F.sum(axis=2)  # F[k, col, row]: column sums over rows
+    x = b.inputs.reshape((b.nb,) + (n,) * d)
+    s = x
+    for i in range(d - 1, -1, -1):
+        s = np.einsum("k...j,kj->k...", s, cs[:, i, :])
+    want = np.zeros(b.n_out)
+    np.add.at(want, b.out_index, s)
+    have = got.sum(axis=1)
+    assert np.linalg.norm(have - want) / np.linalg.norm(want) <= 1e-12
+
+
+def test_linearity_full_config4_f32(cuda):
+    """Full-size configuration 4 in FP32 storage with FP64 outputs: F(2x) = 2 F(x)
+    exactly (scaling by two is exact in binary floating point)."""
+    from kronmult_gb300 import DeviceBatch
+    from kronmult_gb300 import workloads as W
+
+    b = W.config4()
+    db = DeviceBatch.from_host(b, device=cuda, dtype=torch.float32, out_dtype=torch.float64)
+    db.forward()
+    y1 = db.outputs.clone()
+    db.outputs.zero_()
+    db.inputs.mul_(2)
+    db.forward()
+    torch.cuda.synchronize()
+    # the atomic order may differ between the runs; compare normwise
+    assert (torch.linalg.norm(db.outputs - 2 * y1) / torch.linalg.norm(2 * y1)).item() <= 1e-14
