@@ -48,13 +48,15 @@ METRIC = "kron-matvec GFLOP/s"
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--steps", type=int, default=100)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--config", choices=sorted(CONFIGS), default="c2")
     p.add_argument("--dtype", choices=["f64", "f32"], default="f64")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--scale", type=float, default=1.0,
+                   help="shrink the number of outputs/entries (profiling runs only; not a bench value)")
     return p.parse_args()
 
 
@@ -65,13 +67,13 @@ def dist_env():
     return rank, world, local
 
 
-def make_batch(cfg: str, rank: int):
+def make_batch(cfg: str, rank: int, scale: float = 1.0):
     from kronmult_gb300 import workloads as W
 
     fn, _ = CONFIGS[cfg]
     # weak scaling: every rank owns a full-size shard with its own seed (shards are
     # whole output groups, so no data crosses ranks)
-    return getattr(W, fn)(seed=getattr(W, fn).__defaults__[1] + 7919 * rank)
+    return getattr(W, fn)(scale=scale, seed=getattr(W, fn).__defaults__[1] + 7919 * rank)
 
 
 class ClockSampler:
@@ -216,7 +218,7 @@ def main():
     from kronmult_gb300 import DeviceBatch, _lib
 
     lib = _lib.lib()
-    b = make_batch(args.config, rank)
+    b = make_batch(args.config, rank, args.scale)
     tdt = torch.float64 if args.dtype == "f64" else torch.float32
     esize = 8 if args.dtype == "f64" else 4
     db = DeviceBatch.from_host(b, device=dev, dtype=tdt)
@@ -234,6 +236,7 @@ def main():
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
     clocks.start()
+    time.sleep(0.5)  # let nvidia-smi start sampling before the timed region
     barrier()
     torch.cuda.synchronize()
     ev0 = torch.cuda.Event(enable_timing=True)
