@@ -86,6 +86,27 @@ int kronmult_batched_f32_f64out_async(int matrix_count, int matrix_size, const f
                                       double *const *output_batched, float *const *workspace_batched,
                                       int nb_batch, int compute, void *stream, const kronmult_tuning *tuning);
 
+/*
+ * Adjoint of kronmult_batched (no reference counterpart; the reference applied
+ * with transposed factors gives grad_input, kronmult_omp/kronmult.hpp:77-104):
+ *   grad_input_batched[k]          += kron(A_{k,0}^T, ..., A_{k,d-1}^T) . grad_output_batched[k]
+ *   grad_matrix_list_batched[k*d+i] += dL/dA_{k,i}   (n x n, col-major, ld grad_matrix_stride)
+ * where grad_output_batched[k] is the gradient of the output vector entry k adds
+ * into.  Entries that share a factor must share its gradient pointer; the
+ * additions are atomic.  Either gradient table may be NULL to skip it.
+ * Supports 2 <= n <= 8 (cudaErrorNotSupported otherwise).
+ */
+int kronmult_batched_adjoint_f64_async(int matrix_count, int matrix_size, const double *const *matrix_list_batched,
+                                       int matrix_stride, const double *const *input_batched,
+                                       const double *const *grad_output_batched, double *const *grad_input_batched,
+                                       double *const *grad_matrix_list_batched, int grad_matrix_stride,
+                                       int nb_batch, void *stream, const kronmult_tuning *tuning);
+int kronmult_batched_adjoint_f32_async(int matrix_count, int matrix_size, const float *const *matrix_list_batched,
+                                       int matrix_stride, const float *const *input_batched,
+                                       const float *const *grad_output_batched, float *const *grad_input_batched,
+                                       float *const *grad_matrix_list_batched, int grad_matrix_stride,
+                                       int nb_batch, void *stream, const kronmult_tuning *tuning);
+
 /* Diagnostic: measured FP64 FMA throughput of the current GPU in GFLOP/s (no
  * reference counterpart).  Allocates and synchronises; not for use in a graph. */
 int kronmult_diag_fp64_fma_gflops(double *gflops);

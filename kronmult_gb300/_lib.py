@@ -44,6 +44,8 @@ SIGNATURES = {
     "kronmult_batched_f64_async": (_i, [_i, _i, _vp, _i, _vp, _vp, _vp, _i, _vp, _TP]),
     "kronmult_batched_f32_async": (_i, [_i, _i, _vp, _i, _vp, _vp, _vp, _i, _vp, _TP]),
     "kronmult_batched_f32_f64out_async": (_i, [_i, _i, _vp, _i, _vp, _vp, _vp, _i, _i, _vp, _TP]),
+    "kronmult_batched_adjoint_f64_async": (_i, [_i, _i, _vp, _i, _vp, _vp, _vp, _vp, _i, _i, _vp, _TP]),
+    "kronmult_batched_adjoint_f32_async": (_i, [_i, _i, _vp, _i, _vp, _vp, _vp, _vp, _i, _i, _vp, _TP]),
     "kronmult_diag_fp64_fma_gflops": (_i, [ctypes.POINTER(ctypes.c_double)]),
     "kronmult_pow_int": (ctypes.c_longlong, [_i, _i]),
     "kronmult_error_string": (ctypes.c_char_p, [_i]),

@@ -139,6 +139,47 @@ class DeviceBatch:
             raise TypeError(f"unsupported storage/output dtypes {dt}/{self.outputs.dtype}")
 
 
+def adjoint(b: DeviceBatch, grad_outputs: torch.Tensor, grad_inputs: torch.Tensor | None = None,
+            grad_factors: torch.Tensor | None = None, stream=None, tuning=None) -> None:
+    """Adjoint of DeviceBatch.forward on the same batch:
+        grad_inputs[k]                  += kron(A_k)^T . grad_outputs[out_index[k]]
+        grad_factors[fac_index[k]*d + i] += dL/dA_{k,i}   (summed over entries sharing the set)
+    `grad_factors` has the factors' shape (same leading dimension).  Either may be None."""
+    dt = b.inputs.dtype
+    name = {torch.float64: "kronmult_batched_adjoint_f64_async",
+            torch.float32: "kronmult_batched_adjoint_f32_async"}.get(dt)
+    if name is None or b.factors.dtype != dt:
+        raise TypeError("adjoint is defined for float64 and float32 batches")
+    dev = b.inputs.device
+    es = b.inputs.element_size()
+    N = b.N
+    gout = grad_outputs.contiguous()
+    if gout.dtype != dt or gout.shape[1] != N:
+        raise ValueError("grad_outputs must be (n_out, N) of the batch dtype")
+    gout_ptrs = gout.data_ptr() + b.out_index * (N * es)
+    gin_ptrs = None
+    if grad_inputs is not None:
+        if grad_inputs.shape != b.inputs.shape or grad_inputs.dtype != dt or not grad_inputs.is_contiguous():
+            raise ValueError("grad_inputs must match the inputs' shape and dtype")
+        k = torch.arange(b.nb, device=dev, dtype=torch.int64)
+        gin_ptrs = grad_inputs.data_ptr() + k * (N * es)
+    gmat_ptrs = None
+    if grad_factors is not None:
+        if grad_factors.shape != b.factors.shape or grad_factors.dtype != dt or not grad_factors.is_contiguous():
+            raise ValueError("grad_factors must match the factors' shape and dtype")
+        i = torch.arange(b.d, device=dev, dtype=torch.int64)
+        blk = b.factors.shape[1]
+        gmat_ptrs = (grad_factors.data_ptr() + (b.fac_index[:, None] * b.d + i[None, :]) * (blk * es)).reshape(-1)
+    fn = getattr(_lib.lib(), name)
+    st = fn(b.d, b.n, b.mat_ptrs.data_ptr(), b.stride, b.in_ptrs.data_ptr(), gout_ptrs.data_ptr(),
+            None if gin_ptrs is None else gin_ptrs.data_ptr(), None if gmat_ptrs is None else gmat_ptrs.data_ptr(),
+            b.stride, b.nb, _stream_handle(stream), _lib.tuning_ptr(tuning))
+    _lib.check(st, name)
+    # the pointer tables are temporaries: keep them referenced (until the next call on this
+    # batch) so that the caching allocator cannot hand their memory out before the kernel reads it
+    b._keepalive = (gout, gout_ptrs, gin_ptrs, gmat_ptrs)
+
+
 def forward_f32_f64out(b: DeviceBatch, compute: int = _lib.KRONMULT_COMPUTE_FP32, stream=None,
                        tuning=None) -> None:
     """FP32 factors/inputs, FP32 (or TF32/BF16 tensor-core) contraction, FP64 output accumulation."""

@@ -1,0 +1,3 @@
+// Explicit instantiation of the adjoint kernels for float.
+#include "adj_kernels.cuh"
+KGB_ADJ_INSTANTIATE(float)

@@ -1,0 +1,254 @@
+// Adjoint kernels of the batched Kronecker matrix-vector product.
+//
+// Forward (per entry k, output group e = out(k)):  y_k = K_k x_k,
+// K_k = kron(A_{k,0}, ..., A_{k,d-1}).  With g_e = dL/d(output e):
+//   grad_input[k]  += K_k^T g_e = kron(A_{k,0}^T, ..., A_{k,d-1}^T) g_e
+//   grad_A_{k,i}   += G_(i) P_(i)^T          (n x n, summed over entries sharing A)
+// where p_i = (I x .. x I x A_{i+1} x .. x A_{d-1}) x_k  (modes after i applied),
+//       q_i = (A_0^T x .. x A_{i-1}^T x I x .. x I) g_e  (modes before i applied),
+// and G_(i), P_(i) are the mode-i unfoldings of q_i and p_i.  The reference has no
+// adjoint; kronmult_batched applied with transposed factors gives grad_input
+// (kronmult_omp/kronmult.hpp:77-104), which the tests use as the check.
+//
+// Layouts.  The p-sweep is the forward's backward sweep (contract the fastest
+// index, put the result index slowest): after applying modes d-1..i+1 the index
+// order (slowest..fastest) is (j_{i+1}..j_{d-1}, l_0..l_{i-1}, l_i), so
+//     P_(i)[c, t] = p_i[c + n*t].
+// The q-sweep contracts the SLOWEST index and puts the result index fastest:
+//     Z[r + n*t] = sum_k A_i(k, r) Q[t + R*k],   R = N/n,
+// so after modes 0..i-1 the order is (j_i, j_{i+1}..j_{d-1}, l_0..l_{i-1}) and
+//     G_(i)[r, t] = q_i[t + R*r]
+// with the same ordering of the remaining index t as P_(i).  After all d modes q
+// is K^T g in natural order: the grad_input.
+//
+// The forward partial products p_i are recomputed in shared memory rather than
+// stored in global memory: all d of them are kept when they fit, otherwise each
+// one is rebuilt from x when the q-sweep reaches it.
+#pragma once
+#include "fwd_kernels.cuh"
+
+namespace kgb {
+
+template <typename T> struct AdjArgs {
+    const T *const *mats;   // nb*d factor pointers
+    const T *const *in;     // nb forward inputs
+    const T *const *gout;   // nb output-gradient pointers (g of the output entry k adds into)
+    T *const *gin;          // nb grad_input pointers (+=), or null
+    T *const *gmats;        // nb*d grad-factor pointers (+=), or null
+    long long nb;
+    int d, n, stride, gstride;
+    int N;
+    int team_size, teams_per_cta, entries_per_team;
+    int team_elems;         // elements of T per team slice
+    int npad;               // padded vector length
+    int store_all;          // 1: keep all d partial products; 0: rebuild each from x
+    int slices;             // split of the grad contraction over the team
+};
+
+// forward-style mode product (contract fastest index), src -> dst (distinct buffers)
+template <typename T, int NN, int QMAX>
+__device__ __forceinline__ void mode_fast(const T *__restrict__ src, T *__restrict__ dst, const T *M, int F,
+                                          const Team &tm)
+{
+#pragma unroll
+    for (int q = 0; q < QMAX; ++q) {
+        const int c = tm.rank + q * tm.size;
+        if (c < F) {
+            T xv[NN];
+            load_fibre<T, NN>(src + c * NN, xv);
+#pragma unroll
+            for (int r = 0; r < NN; ++r) {
+                T s = T(0);
+#pragma unroll
+                for (int k = 0; k < NN; ++k) s = fma_t<T>(M[r + k * NN], xv[k], s);
+                dst[c + r * F] = s;
+            }
+        }
+    }
+}
+
+// transposed mode product contracting the slowest index, in place through registers:
+// Z[r + n*t] = sum_k A(k, r) Q[t + R*k]
+template <typename T, int NN, int QMAX>
+__device__ __forceinline__ void mode_slow_inplace(T *buf, const T *M, int R, const Team &tm)
+{
+    T z[QMAX][NN];
+#pragma unroll
+    for (int q = 0; q < QMAX; ++q) {
+        const int t = tm.rank + q * tm.size;
+        if (t < R) {
+            T qv[NN];
+#pragma unroll
+            for (int k = 0; k < NN; ++k) qv[k] = buf[t + R * k];
+#pragma unroll
+            for (int r = 0; r < NN; ++r) {
+                T s = T(0);
+#pragma unroll
+                for (int k = 0; k < NN; ++k) s = fma_t<T>(M[k + r * NN], qv[k], s);
+                z[q][r] = s;
+            }
+        }
+    }
+    tm.sync();
+#pragma unroll
+    for (int q = 0; q < QMAX; ++q) {
+        const int t = tm.rank + q * tm.size;
+        if (t < R) {
+#pragma unroll
+            for (int r = 0; r < NN; ++r) buf[r + NN * t] = z[q][r];
+        }
+    }
+    tm.sync();
+}
+
+template <typename T, int NN, int QMAX>
+__global__ void __launch_bounds__(512) adj_smem_kernel(const AdjArgs<T> a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const Team tm(a.team_size);
+    constexpr int P = NN * NN;
+    const int N = a.N, d = a.d, R = N / NN;
+    T *base = reinterpret_cast<T *>(smem_raw) + (size_t)tm.id * a.team_elems;
+    // slice layout: [p buffers][q][fac d*P][gacc d*P][gpart slices*P][cur grad pointers d]
+    const int np = a.store_all ? d : 3;
+    T *pb = base;
+    T *qb = pb + (size_t)np * a.npad;
+    T *fac = qb + a.npad;
+    T *gacc = fac + d * P;
+    T *gpart = gacc + d * P;
+    T **curp = reinterpret_cast<T **>(gpart + a.slices * P + ((a.slices * P) & 1));
+    const bool want_gin = a.gin != nullptr;
+    const bool want_gA = a.gmats != nullptr;
+
+    const long long team_global = (long long)blockIdx.x * a.teams_per_cta + tm.id;
+    long long e = team_global * a.entries_per_team;
+    const long long e_end = min(e + (long long)a.entries_per_team, a.nb);
+    if (e >= e_end) return;
+
+    if (want_gA) {
+        for (int v = tm.rank; v < d * P; v += tm.size) gacc[v] = T(0);
+        for (int v = tm.rank; v < d; v += tm.size) curp[v] = nullptr;
+    }
+    tm.sync();
+
+    for (; e < e_end; ++e) {
+        // flush grad accumulators whose target changes with this entry
+        if (want_gA) {
+            for (int v = tm.rank; v < d * P; v += tm.size) {
+                const int i = v / P, pr = v - i * P;
+                T *gp = a.gmats[e * d + i];
+                T *cp = curp[i];
+                if (gp != cp) {
+                    if (cp != nullptr) {
+                        const int r = pr % NN, c = pr / NN;
+                        atomic_add<T>(cp + r + (size_t)c * a.gstride, gacc[v]);
+                    }
+                    gacc[v] = T(0);
+                }
+            }
+            tm.sync();
+            for (int v = tm.rank; v < d; v += tm.size) curp[v] = a.gmats[e * d + v];
+        }
+        // stage x (as p_{d-1}), g, and the factors
+        T *xbuf = a.store_all ? pb + (size_t)(d - 1) * a.npad : pb;
+        stage_vector(xbuf, a.in[e], N, tm);
+        stage_vector(qb, a.gout[e], N, tm);
+        stage_factors<T, NN>(fac, a.mats + e * d, d, a.stride, tm);
+        tm.sync();
+        if (a.store_all) {
+            for (int i = d - 1; i >= 1; --i) {
+                mode_fast<T, NN, QMAX>(pb + (size_t)i * a.npad, pb + (size_t)(i - 1) * a.npad, fac + i * P, R, tm);
+                tm.sync();
+            }
+        }
+        for (int i = 0; i < d; ++i) {
+            if (want_gA) {
+                const T *pi;
+                if (a.store_all) {
+                    pi = pb + (size_t)i * a.npad;
+                } else {
+                    // rebuild p_i = modes d-1..i+1 applied to x, ping-ponging pb[1] and pb[2]
+                    const T *src = pb;
+                    T *dst = pb + a.npad;
+                    for (int m = d - 1; m > i; --m) {
+                        mode_fast<T, NN, QMAX>(src, dst, fac + m * P, R, tm);
+                        tm.sync();
+                        src = dst;
+                        dst = (dst == pb + a.npad) ? pb + 2 * (size_t)a.npad : pb + a.npad;
+                    }
+                    pi = src;
+                }
+                // partial G_(i) P_(i)^T over slices of t
+                const int S = a.slices;
+                const int tlen = (R + S - 1) / S;
+                for (int w = tm.rank; w < S * P; w += tm.size) {
+                    const int pr = w % P, sl = w / P;
+                    const int r = pr % NN, c = pr / NN;
+                    const int t0 = sl * tlen, t1 = min(R, t0 + tlen);
+                    T s = T(0);
+                    for (int t = t0; t < t1; ++t) s = fma_t<T>(qb[t + R * r], pi[c + NN * t], s);
+                    gpart[w] = s;
+                }
+                tm.sync();
+                for (int pr = tm.rank; pr < P; pr += tm.size) {
+                    T s = T(0);
+                    for (int sl = 0; sl < S; ++sl) s += gpart[sl * P + pr];
+                    gacc[i * P + pr] += s;
+                }
+            }
+            if (i < d - 1 || want_gin) mode_slow_inplace<T, NN, QMAX>(qb, fac + i * P, R, tm);
+        }
+        if (want_gin) {
+            T *gi = a.gin[e];
+            for (int v = tm.rank; v < N; v += tm.size) atomic_add<T>(gi + v, qb[v]);
+        }
+        tm.sync();
+    }
+    if (want_gA) {
+        tm.sync();
+        for (int v = tm.rank; v < d * P; v += tm.size) {
+            const int i = v / P, pr = v - i * P;
+            T *cp = curp[i];
+            if (cp != nullptr) {
+                const int r = pr % NN, c = pr / NN;
+                atomic_add<T>(cp + r + (size_t)c * a.gstride, gacc[v]);
+            }
+        }
+    }
+}
+
+template <typename T> using AdjFn = void (*)(const AdjArgs<T>);
+template <typename T> AdjFn<T> adj_lookup(int nn, int qmax);
+
+}  // namespace kgb
+
+#define KGB_ADJ_INSTANTIATE(T)                                                                         \
+    namespace kgb {                                                                                    \
+    template <> AdjFn<T> adj_lookup<T>(int nn, int qmax)                                               \
+    {                                                                                                  \
+        switch (nn * 16 + qmax) {                                                                      \
+        case 2 * 16 + 1: return adj_smem_kernel<T, 2, 1>;                                              \
+        case 2 * 16 + 2: return adj_smem_kernel<T, 2, 2>;                                              \
+        case 2 * 16 + 4: return adj_smem_kernel<T, 2, 4>;                                              \
+        case 3 * 16 + 1: return adj_smem_kernel<T, 3, 1>;                                              \
+        case 3 * 16 + 2: return adj_smem_kernel<T, 3, 2>;                                              \
+        case 3 * 16 + 4: return adj_smem_kernel<T, 3, 4>;                                              \
+        case 4 * 16 + 1: return adj_smem_kernel<T, 4, 1>;                                              \
+        case 4 * 16 + 2: return adj_smem_kernel<T, 4, 2>;                                              \
+        case 4 * 16 + 4: return adj_smem_kernel<T, 4, 4>;                                              \
+        case 5 * 16 + 1: return adj_smem_kernel<T, 5, 1>;                                              \
+        case 5 * 16 + 2: return adj_smem_kernel<T, 5, 2>;                                              \
+        case 5 * 16 + 4: return adj_smem_kernel<T, 5, 4>;                                              \
+        case 6 * 16 + 1: return adj_smem_kernel<T, 6, 1>;                                              \
+        case 6 * 16 + 2: return adj_smem_kernel<T, 6, 2>;                                              \
+        case 6 * 16 + 4: return adj_smem_kernel<T, 6, 4>;                                              \
+        case 7 * 16 + 1: return adj_smem_kernel<T, 7, 1>;                                              \
+        case 7 * 16 + 2: return adj_smem_kernel<T, 7, 2>;                                              \
+        case 7 * 16 + 4: return adj_smem_kernel<T, 7, 4>;                                              \
+        case 8 * 16 + 1: return adj_smem_kernel<T, 8, 1>;                                              \
+        case 8 * 16 + 2: return adj_smem_kernel<T, 8, 2>;                                              \
+        case 8 * 16 + 4: return adj_smem_kernel<T, 8, 4>;                                              \
+        default: return nullptr;                                                                       \
+        }                                                                                              \
+    }                                                                                                  \
+    }

@@ -2,6 +2,7 @@
 #include <map>
 #include <mutex>
 #include <utility>
+#include "adj_kernels.cuh"
 #include "fwd_launch.cuh"
 
 namespace kgb {
@@ -72,6 +73,97 @@ static int forward_async(int d, int n, const T *const *mats, int stride, const T
     return launch_plan<T, TO>(pl, st);
 }
 
+template <typename T>
+static int adjoint_async(int d, int n, const T *const *mats, int stride, const T *const *in, const T *const *gout,
+                         T *const *gin, T *const *gmats, int gstride, long long nb, cudaStream_t st,
+                         const kronmult_tuning *tune)
+{
+    if (d < 0 || n < 0 || nb < 0) return cudaErrorInvalidValue;
+    if (stride < (n > 0 ? n : 1)) return cudaErrorInvalidValue;
+    if (gmats && gstride < (n > 0 ? n : 1)) return cudaErrorInvalidValue;
+    const long long Nl = pow_ll(n, d);
+    if (Nl > (long long)INT_MAX) return cudaErrorInvalidValue;
+    if (nb == 0 || n == 0 || (!gin && !gmats)) return cudaSuccess;
+    if (!mats || !in || !gout) return cudaErrorInvalidValue;
+    if (n < 2 || n > 8 || d < 1) return cudaErrorNotSupported;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return cudaErrorInvalidDevice;
+    const DeviceInfo &di = device_info(dev);
+    const int N = (int)Nl, R = N / n, P = n * n;
+    int ts = 8;
+    if (tune && tune->team_size > 0) {
+        ts = tune->team_size;
+    } else {
+        while (ts < 512 && ts * 2 < R) ts *= 2;
+    }
+    const int q = (R + ts - 1) / ts;
+    int qmax = 1;
+    while (qmax < q) qmax *= 2;
+    if (qmax > 4) return cudaErrorNotSupported;
+    auto fn = adj_lookup<T>(n, qmax);
+    if (!fn) return cudaErrorNotSupported;
+    const int align = 16 / (int)sizeof(T);
+    const int npad = round_up(N, align);
+    int slices = ts / P;
+    if (slices < 1) slices = 1;
+    if (slices > R) slices = R;
+    auto team_elems_for = [&](int store_all) {
+        const int np = store_all ? d : 3;
+        const int ptr_elems = (8 * d + (int)sizeof(T) - 1) / (int)sizeof(T);
+        return round_up(np * npad + npad + 2 * d * P + slices * P + 1 + ptr_elems, align);
+    };
+    int block = ts >= 256 ? ts : 256;
+    int teams = block / ts;
+    while (ts >= 64 && ts < block && teams > 15) {
+        block /= 2;
+        teams = block / ts;
+    }
+    int store_all = 1;
+    size_t team_bytes = (size_t)team_elems_for(1) * sizeof(T);
+    if (team_bytes > (size_t)di.max_smem_optin) {
+        store_all = 0;
+        team_bytes = (size_t)team_elems_for(0) * sizeof(T);
+        if (team_bytes > (size_t)di.max_smem_optin) return cudaErrorNotSupported;
+    }
+    while (teams > 1 && (size_t)teams * team_bytes > (size_t)di.max_smem_optin) {
+        block /= 2;
+        teams = block / ts;
+    }
+    if (block < 32) block = 32, teams = block / ts;
+    const size_t smem = (size_t)teams * team_bytes;
+    if (!ensure_smem_attr((const void *)fn, smem)) return cudaErrorInvalidValue;
+    int per_sm = (tune && tune->ctas_per_sm > 0) ? tune->ctas_per_sm : occupancy((const void *)fn, block, smem);
+    if (per_sm < 1) per_sm = 1;
+    const long long total_teams = (long long)di.sms * per_sm * teams;
+    long long ept = (tune && tune->entries_per_team > 0) ? tune->entries_per_team
+                                                         : (nb + total_teams - 1) / total_teams;
+    if (ept < 1) ept = 1;
+    if (ept > INT_MAX) ept = INT_MAX;
+    const long long grid = (nb + ept * teams - 1) / (ept * teams);
+    if (grid > INT_MAX) return cudaErrorInvalidValue;
+    AdjArgs<T> a{};
+    a.mats = mats;
+    a.in = in;
+    a.gout = gout;
+    a.gin = gin;
+    a.gmats = gmats;
+    a.nb = nb;
+    a.d = d;
+    a.n = n;
+    a.stride = stride;
+    a.gstride = gstride;
+    a.N = N;
+    a.team_size = ts;
+    a.teams_per_cta = teams;
+    a.entries_per_team = (int)ept;
+    a.team_elems = (int)(team_bytes / sizeof(T));
+    a.npad = npad;
+    a.store_all = store_all;
+    a.slices = slices;
+    fn<<<(unsigned)grid, block, smem, st>>>(a);
+    return (int)cudaGetLastError();
+}
+
 }  // namespace kgb
 
 using namespace kgb;
@@ -129,6 +221,28 @@ int kronmult_batched_f32_f64out_async(int matrix_count, int matrix_size, const f
     return forward_async<float, double>(matrix_count, matrix_size, matrix_list_batched, matrix_stride,
                                         input_batched, output_batched, workspace_batched, nb_batch,
                                         (cudaStream_t)stream, tuning);
+}
+
+int kronmult_batched_adjoint_f64_async(int matrix_count, int matrix_size, const double *const *matrix_list_batched,
+                                       int matrix_stride, const double *const *input_batched,
+                                       const double *const *grad_output_batched, double *const *grad_input_batched,
+                                       double *const *grad_matrix_list_batched, int grad_matrix_stride,
+                                       int nb_batch, void *stream, const kronmult_tuning *tuning)
+{
+    return adjoint_async<double>(matrix_count, matrix_size, matrix_list_batched, matrix_stride, input_batched,
+                                 grad_output_batched, grad_input_batched, grad_matrix_list_batched,
+                                 grad_matrix_stride, nb_batch, (cudaStream_t)stream, tuning);
+}
+
+int kronmult_batched_adjoint_f32_async(int matrix_count, int matrix_size, const float *const *matrix_list_batched,
+                                       int matrix_stride, const float *const *input_batched,
+                                       const float *const *grad_output_batched, float *const *grad_input_batched,
+                                       float *const *grad_matrix_list_batched, int grad_matrix_stride,
+                                       int nb_batch, void *stream, const kronmult_tuning *tuning)
+{
+    return adjoint_async<float>(matrix_count, matrix_size, matrix_list_batched, matrix_stride, input_batched,
+                                grad_output_batched, grad_input_batched, grad_matrix_list_batched,
+                                grad_matrix_stride, nb_batch, (cudaStream_t)stream, tuning);
 }
 
 long long kronmult_pow_int(int number, int power) { return pow_ll(number, power); }
