@@ -41,6 +41,15 @@ extern "C" {
 #define KRONMULT_COMPUTE_TF32 1 /* TF32 tensor-core mode products (n == 8), FP32 accumulate */
 #define KRONMULT_COMPUTE_BF16 2 /* BF16 tensor-core mode products (n == 8), FP32 accumulate */
 
+/* Storage/output type codes. */
+#define KRONMULT_DTYPE_F64 0        /* double factors, inputs and outputs */
+#define KRONMULT_DTYPE_F32 1        /* float factors, inputs and outputs */
+#define KRONMULT_DTYPE_F32_F64OUT 2 /* float factors and inputs, double outputs */
+
+/* Output modes of the grouped entry point. */
+#define KRONMULT_MODE_ATOMIC 0        /* atomic additions into shared outputs */
+#define KRONMULT_MODE_DETERMINISTIC 1 /* segmented reduction per output pointer, bitwise reproducible */
+
 /* Launch shape override used by the autotuner; zero fields mean "heuristic". */
 typedef struct kronmult_tuning {
     int team_size;        /* threads cooperating on one entry: 8,16,...,512 */
@@ -106,6 +115,50 @@ int kronmult_batched_adjoint_f32_async(int matrix_count, int matrix_size, const 
                                        const float *const *grad_output_batched, float *const *grad_input_batched,
                                        float *const *grad_matrix_list_batched, int grad_matrix_stride,
                                        int nb_batch, void *stream, const kronmult_tuning *tuning);
+
+/*
+ * Grouped persistent forward (no reference counterpart; the reference serves one
+ * (d, n) per call, kronmult_gpu/kronmult.cu:173-197).  Each group is one
+ * kronmult_batched call's worth of arguments (device pointer tables).  A plan is
+ * built once -- it reads the output pointer tables, orders the entries of each
+ * group by output pointer for the deterministic mode, cuts the work into items
+ * and uploads them -- and kronmult_grouped_run then enqueues one persistent
+ * kernel that pulls the items from a device queue.  The run only enqueues a
+ * memset and a kernel, so it can be captured in a CUDA graph.  Rebuild the plan
+ * if the pointer tables change.  In the deterministic mode no output vector may
+ * be shared between groups (cudaErrorInvalidValue).  Supports 2 <= n <= 8 with
+ * n^d small enough for one team's shared memory (cudaErrorNotSupported otherwise).
+ */
+typedef struct kronmult_group {
+    int matrix_count, matrix_size, matrix_stride, nb_batch;
+    const void *const *matrix_list_batched; /* nb*d device pointers */
+    const void *const *input_batched;       /* nb device pointers */
+    void *const *output_batched;            /* nb device pointers (may alias) */
+} kronmult_group;
+
+typedef struct kronmult_grouped_plan_s *kronmult_grouped_plan;
+
+int kronmult_grouped_plan_create(kronmult_grouped_plan *plan, const kronmult_group *groups, int n_groups, int dtype,
+                                 int mode, const kronmult_tuning *tunings);
+int kronmult_grouped_run(kronmult_grouped_plan plan, void *stream);
+/* info[0..5] = grid, block, dynamic shared bytes, queue items, team ranges, permuted entries */
+int kronmult_grouped_plan_info(kronmult_grouped_plan plan, long long *info, int n_info);
+int kronmult_grouped_plan_destroy(kronmult_grouped_plan plan);
+
+/*
+ * Autotuner (no reference counterpart): times every valid launch shape of the
+ * forward for (matrix_count, matrix_size, dtype) on a synthetic batch of
+ * nb_sample entries (0 = enough to exceed L2), stores the fastest in the
+ * process-wide tuning cache and returns it.  Allocates and synchronises.
+ * kronmult_batched* and the grouped planner use the cache when given no tuning.
+ */
+int kronmult_autotune_forward(int matrix_count, int matrix_size, int dtype, int nb_sample, kronmult_tuning *best,
+                              float *best_ms);
+int kronmult_tuning_cache_get(int matrix_count, int matrix_size, int dtype, kronmult_tuning *out);
+int kronmult_tuning_cache_set(int matrix_count, int matrix_size, int dtype, const kronmult_tuning *t);
+int kronmult_tuning_cache_clear(void);
+int kronmult_tuning_cache_save(const char *path);
+int kronmult_tuning_cache_load(const char *path);
 
 /* Diagnostic: measured FP64 FMA throughput of the current GPU in GFLOP/s (no
  * reference counterpart).  Allocates and synchronises; not for use in a graph. */

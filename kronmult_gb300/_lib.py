@@ -22,6 +22,21 @@ class Tuning(ctypes.Structure):
     _fields_ = [("team_size", ctypes.c_int), ("ctas_per_sm", ctypes.c_int), ("entries_per_team", ctypes.c_int)]
 
 
+class Group(ctypes.Structure):
+    """Mirror of `kronmult_group`: one group's arguments (device pointer tables)."""
+
+    _fields_ = [("matrix_count", ctypes.c_int), ("matrix_size", ctypes.c_int), ("matrix_stride", ctypes.c_int),
+                ("nb_batch", ctypes.c_int), ("matrix_list_batched", ctypes.c_void_p),
+                ("input_batched", ctypes.c_void_p), ("output_batched", ctypes.c_void_p)]
+
+
+KRONMULT_DTYPE_F64 = 0
+KRONMULT_DTYPE_F32 = 1
+KRONMULT_DTYPE_F32_F64OUT = 2
+KRONMULT_MODE_ATOMIC = 0
+KRONMULT_MODE_DETERMINISTIC = 1
+
+
 class KronmultError(RuntimeError):
     """A non-zero status (a cudaError_t value) returned by the library."""
 
@@ -46,6 +61,17 @@ SIGNATURES = {
     "kronmult_batched_f32_f64out_async": (_i, [_i, _i, _vp, _i, _vp, _vp, _vp, _i, _i, _vp, _TP]),
     "kronmult_batched_adjoint_f64_async": (_i, [_i, _i, _vp, _i, _vp, _vp, _vp, _vp, _i, _i, _vp, _TP]),
     "kronmult_batched_adjoint_f32_async": (_i, [_i, _i, _vp, _i, _vp, _vp, _vp, _vp, _i, _i, _vp, _TP]),
+    "kronmult_grouped_plan_create": (_i, [ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(Group), _i, _i, _i,
+                                         _TP]),
+    "kronmult_grouped_run": (_i, [_vp, _vp]),
+    "kronmult_grouped_plan_info": (_i, [_vp, ctypes.POINTER(ctypes.c_longlong), _i]),
+    "kronmult_grouped_plan_destroy": (_i, [_vp]),
+    "kronmult_autotune_forward": (_i, [_i, _i, _i, _i, _TP, ctypes.POINTER(ctypes.c_float)]),
+    "kronmult_tuning_cache_get": (_i, [_i, _i, _i, _TP]),
+    "kronmult_tuning_cache_set": (_i, [_i, _i, _i, _TP]),
+    "kronmult_tuning_cache_clear": (_i, []),
+    "kronmult_tuning_cache_save": (_i, [ctypes.c_char_p]),
+    "kronmult_tuning_cache_load": (_i, [ctypes.c_char_p]),
     "kronmult_diag_fp64_fma_gflops": (_i, [ctypes.POINTER(ctypes.c_double)]),
     "kronmult_pow_int": (ctypes.c_longlong, [_i, _i]),
     "kronmult_error_string": (ctypes.c_char_p, [_i]),

@@ -96,6 +96,8 @@ static int adjoint_async(int d, int n, const T *const *mats, int stride, const T
     } else {
         while (ts < 512 && ts * 2 < R) ts *= 2;
     }
+    if (ts < 8 || ts > 512 || (ts & (ts - 1))) return cudaErrorInvalidValue;
+    while (ts < 512 && (R + ts - 1) / ts > 4) ts *= 2;  // a requested team too small for 4 fibres/thread grows
     const int q = (R + ts - 1) / ts;
     int qmax = 1;
     while (qmax < q) qmax *= 2;

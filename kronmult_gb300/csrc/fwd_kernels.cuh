@@ -98,36 +98,51 @@ template <typename T, int NN> __device__ __forceinline__ void load_fibre(const T
 template <typename T> __device__ __forceinline__ T fma_t(T a, T b, T c) { return fma(a, b, c); }
 template <> __device__ __forceinline__ float fma_t<float>(float a, float b, float c) { return fmaf(a, b, c); }
 
-// ---- shared-memory, register in-place kernel (compile-time n) -------------
+// ---- shared-memory, register in-place team forward (compile-time n) -------
 //
 // Thread `rank` of a team owns fibres c = rank + q*team_size (q < QMAX) in every
 // mode and computes all n outputs of each of its fibres, so each staged input
 // value is read from shared memory once per mode.  The mode is done in place:
 // every thread reads its fibres into registers, the team synchronises, and the
 // results are written to their rotated positions c + r*F.
-template <typename T, typename TO, int NN, int QMAX>
-__global__ void __launch_bounds__(512) fwd_smem_kernel(const FwdArgs<T, TO> a)
+//
+// The team walks entries [e_begin, e_end) (through `perm` when given) and sums
+// consecutive entries with the same output pointer in registers.  A run is
+// flushed with atomic adds, or -- in deterministic mode, where the caller
+// guarantees that every output pointer is one contiguous run owned by this team --
+// with a plain read-modify-write, so that the sum order is the entry order.
+template <typename T, typename TO, int NN, int QMAX, bool DET>
+__device__ __forceinline__ void team_forward(const T *const *mats, const T *const *in, TO *const *out,
+                                             const long long *perm, int d, int stride, int N, long long e_begin,
+                                             long long e_end, T *buf, T *fac, const Team &tm)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const Team tm(a.team_size);
-    T *buf = reinterpret_cast<T *>(smem_raw) + (size_t)tm.id * a.team_elems;
-    T *fac = buf + a.vec_pad;
-    const int N = a.N;
     const int F = N / NN;
-    const int d = a.d;
-
-    const long long team_global = (long long)blockIdx.x * a.teams_per_cta + tm.id;
-    long long e = team_global * a.entries_per_team;
-    const long long e_end = min(e + (long long)a.entries_per_team, a.nb);
-
     TO acc[QMAX][NN];
     TO *cur = nullptr;
 
-    for (; e < e_end; ++e) {
-        const T *x = a.in[e];
-        TO *o = a.out[e];
+    auto flush = [&](TO *dst) {
+#pragma unroll
+        for (int q = 0; q < QMAX; ++q) {
+            const int c = tm.rank + q * tm.size;
+            if (c < F) {
+#pragma unroll
+                for (int r = 0; r < NN; ++r) {
+                    if constexpr (DET) {
+                        dst[c + r * F] = dst[c + r * F] + acc[q][r];
+                    } else {
+                        atomic_add<TO>(dst + c + r * F, acc[q][r]);
+                    }
+                }
+            }
+        }
+    };
+
+    for (long long ei = e_begin; ei < e_end; ++ei) {
+        const long long e = perm ? perm[ei] : ei;
+        const T *x = in[e];
+        TO *o = out[e];
         stage_vector(buf, x, N, tm);
-        stage_factors<T, NN>(fac, a.mats + e * d, d, a.stride, tm);
+        stage_factors<T, NN>(fac, mats + e * d, d, stride, tm);
         tm.sync();
 
         T y[QMAX][NN];
@@ -174,16 +189,7 @@ __global__ void __launch_bounds__(512) fwd_smem_kernel(const FwdArgs<T, TO> a)
         }
         // y[q][r] is element c + r*F of kron(A) . x
         if (o != cur) {
-            if (cur != nullptr) {
-#pragma unroll
-                for (int q = 0; q < QMAX; ++q) {
-                    const int c = tm.rank + q * tm.size;
-                    if (c < F) {
-#pragma unroll
-                        for (int r = 0; r < NN; ++r) atomic_add<TO>(cur + c + r * F, acc[q][r]);
-                    }
-                }
-            }
+            if (cur != nullptr) flush(cur);
             cur = o;
 #pragma unroll
             for (int q = 0; q < QMAX; ++q)
@@ -196,16 +202,20 @@ __global__ void __launch_bounds__(512) fwd_smem_kernel(const FwdArgs<T, TO> a)
                 for (int r = 0; r < NN; ++r) acc[q][r] += (TO)y[q][r];
         }
     }
-    if (cur != nullptr) {
-#pragma unroll
-        for (int q = 0; q < QMAX; ++q) {
-            const int c = tm.rank + q * tm.size;
-            if (c < F) {
-#pragma unroll
-                for (int r = 0; r < NN; ++r) atomic_add<TO>(cur + c + r * F, acc[q][r]);
-            }
-        }
-    }
+    if (cur != nullptr) flush(cur);
+}
+
+template <typename T, typename TO, int NN, int QMAX>
+__global__ void __launch_bounds__(512) fwd_smem_kernel(const FwdArgs<T, TO> a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const Team tm(a.team_size);
+    T *buf = reinterpret_cast<T *>(smem_raw) + (size_t)tm.id * a.team_elems;
+    T *fac = buf + a.vec_pad;
+    const long long team_global = (long long)blockIdx.x * a.teams_per_cta + tm.id;
+    const long long e = team_global * a.entries_per_team;
+    const long long e_end = min(e + (long long)a.entries_per_team, a.nb);
+    team_forward<T, TO, NN, QMAX, false>(a.mats, a.in, a.out, nullptr, a.d, a.stride, a.N, e, e_end, buf, fac, tm);
 }
 
 // ---- generic kernel (runtime n, any N) ------------------------------------

@@ -5,6 +5,7 @@
 #include <mutex>
 #include "fwd_kernels.cuh"
 #include "kronmult_gb300.h"
+#include "tuning.cuh"
 
 namespace kgb {
 
@@ -64,6 +65,12 @@ int plan_forward(FwdPlan<T, TO> &pl, int d, int n, const T *const *mats, int str
     if (Nl > (long long)INT_MAX) return cudaErrorInvalidValue;
     pl.args = FwdArgs<T, TO>{};
     pl.fn = nullptr;
+    kronmult_tuning cached{};
+    if (!tune) {
+        const int code = sizeof(T) == 8 ? KRONMULT_DTYPE_F64
+                                        : (sizeof(TO) == 8 ? KRONMULT_DTYPE_F32_F64OUT : KRONMULT_DTYPE_F32);
+        if (tuning_cache_lookup(d, n, code, cached)) tune = &cached;
+    }
     if (nb == 0 || n == 0) return cudaSuccess;  // nothing to add
     if (!in || !out || (d > 0 && !mats)) return cudaErrorInvalidValue;
 

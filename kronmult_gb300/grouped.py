@@ -1,0 +1,108 @@
+"""Grouped persistent forward and the autotuner, over the C ABI.
+
+`GroupedPlan([batch, ...], mode)` builds one plan for several DeviceBatch groups
+of different (d, n, fan-in); `plan.run(stream)` enqueues the single persistent
+launch (graph-capturable).  mode "atomic" adds with atomics; "deterministic"
+sums every output's entries in entry order and writes each output once, so the
+result is bitwise reproducible.
+
+`autotune_forward(d, n, dtype)` times the forward's launch shapes on the GPU and
+stores the fastest in the library's tuning cache, which the planners consult.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import torch
+
+from . import _lib
+from .api import DeviceBatch, _stream_handle
+
+MODES = {"atomic": _lib.KRONMULT_MODE_ATOMIC, "deterministic": _lib.KRONMULT_MODE_DETERMINISTIC}
+DTYPES = {torch.float64: _lib.KRONMULT_DTYPE_F64, torch.float32: _lib.KRONMULT_DTYPE_F32}
+
+
+class GroupedPlan:
+    def __init__(self, batches: list[DeviceBatch], mode: str = "atomic", tunings: list[dict] | None = None):
+        if not batches:
+            raise ValueError("at least one group is needed")
+        dt = batches[0].inputs.dtype
+        for b in batches:
+            if b.inputs.dtype != dt or b.outputs.dtype != dt or b.factors.dtype != dt:
+                raise TypeError("all groups must share one dtype (float64 or float32)")
+        if dt not in DTYPES:
+            raise TypeError("grouped forward is defined for float64 and float32")
+        self.batches = list(batches)  # keeps the pointer tables alive
+        self.mode = mode
+        groups = (_lib.Group * len(batches))()
+        for g, b in zip(groups, batches):
+            g.matrix_count, g.matrix_size, g.matrix_stride, g.nb_batch = b.d, b.n, b.stride, b.nb
+            g.matrix_list_batched = b.mat_ptrs.data_ptr()
+            g.input_batched = b.in_ptrs.data_ptr()
+            g.output_batched = b.out_ptrs.data_ptr()
+        tp = None
+        if tunings is not None:
+            arr = (_lib.Tuning * len(batches))()
+            for a, t in zip(arr, tunings):
+                t = t or {}
+                a.team_size = int(t.get("team_size", 0))
+                a.ctas_per_sm = int(t.get("ctas_per_sm", 0))
+                a.entries_per_team = int(t.get("entries_per_team", 0))
+            tp = arr
+        self._h = ctypes.c_void_p()
+        st = _lib.lib().kronmult_grouped_plan_create(ctypes.byref(self._h), groups, len(batches), DTYPES[dt],
+                                                      MODES[mode], tp)
+        _lib.check(st, "kronmult_grouped_plan_create")
+
+    def run(self, stream=None) -> None:
+        _lib.check(_lib.lib().kronmult_grouped_run(self._h, _stream_handle(stream)), "kronmult_grouped_run")
+
+    def info(self) -> dict:
+        v = (ctypes.c_longlong * 6)()
+        _lib.check(_lib.lib().kronmult_grouped_plan_info(self._h, v, 6), "kronmult_grouped_plan_info")
+        return dict(zip(("grid", "block", "smem", "items", "ranges", "permuted"), list(v)))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            _lib.lib().kronmult_grouped_plan_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def autotune_forward(d: int, n: int, dtype: int = _lib.KRONMULT_DTYPE_F64, nb_sample: int = 0):
+    """Time the forward's launch shapes for (d, n, dtype); return (tuning dict, best ms)."""
+    t = _lib.Tuning()
+    ms = ctypes.c_float(0)
+    _lib.check(_lib.lib().kronmult_autotune_forward(d, n, dtype, nb_sample, ctypes.byref(t), ctypes.byref(ms)),
+               "kronmult_autotune_forward")
+    return {"team_size": t.team_size, "ctas_per_sm": t.ctas_per_sm, "entries_per_team": t.entries_per_team}, ms.value
+
+
+def tuning_cache_get(d: int, n: int, dtype: int = _lib.KRONMULT_DTYPE_F64):
+    t = _lib.Tuning()
+    if _lib.lib().kronmult_tuning_cache_get(d, n, dtype, ctypes.byref(t)) != 0:
+        return None
+    return {"team_size": t.team_size, "ctas_per_sm": t.ctas_per_sm, "entries_per_team": t.entries_per_team}
+
+
+def tuning_cache_set(d: int, n: int, dtype: int, tuning: dict) -> None:
+    t = _lib.Tuning(int(tuning.get("team_size", 0)), int(tuning.get("ctas_per_sm", 0)),
+                    int(tuning.get("entries_per_team", 0)))
+    _lib.check(_lib.lib().kronmult_tuning_cache_set(d, n, dtype, ctypes.byref(t)), "kronmult_tuning_cache_set")
+
+
+def tuning_cache_clear() -> None:
+    _lib.lib().kronmult_tuning_cache_clear()
+
+
+def tuning_cache_save(path: str) -> None:
+    _lib.check(_lib.lib().kronmult_tuning_cache_save(path.encode()), "kronmult_tuning_cache_save")
+
+
+def tuning_cache_load(path: str) -> None:
+    _lib.check(_lib.lib().kronmult_tuning_cache_load(path.encode()), "kronmult_tuning_cache_load")

@@ -91,3 +91,32 @@ def test_python_mirror_raises(lib):
         import torch
 
         K.kronmult_batched(2, 4, 8, 4, 8, 8, None, 1, dtype=torch.float16)
+
+
+def test_grouped_plan_rejects_bad_mode_and_dtype(lib):
+    import ctypes
+
+    from kronmult_gb300 import _lib
+
+    h = ctypes.c_void_p()
+    g = (_lib.Group * 1)()
+    assert lib.kronmult_grouped_plan_create(ctypes.byref(h), g, 1, 7, 0, None) == CUDA_ERROR_INVALID_VALUE
+    assert lib.kronmult_grouped_plan_create(ctypes.byref(h), g, 1, 0, 9, None) == CUDA_ERROR_INVALID_VALUE
+    assert lib.kronmult_grouped_plan_create(None, g, 1, 0, 0, None) == CUDA_ERROR_INVALID_VALUE
+    assert lib.kronmult_grouped_run(None, None) == CUDA_ERROR_INVALID_VALUE
+    assert lib.kronmult_grouped_plan_destroy(None) == 0
+
+
+def test_tuning_cache_roundtrip_on_host(lib, tmp_path):
+    from kronmult_gb300 import grouped as G
+
+    G.tuning_cache_clear()
+    G.tuning_cache_set(5, 3, 0, {"team_size": 64, "entries_per_team": 4})
+    assert G.tuning_cache_get(5, 3, 0) == {"team_size": 64, "ctas_per_sm": 0, "entries_per_team": 4}
+    path = str(tmp_path / "t.txt")
+    G.tuning_cache_save(path)
+    G.tuning_cache_clear()
+    assert G.tuning_cache_get(5, 3, 0) is None
+    G.tuning_cache_load(path)
+    assert G.tuning_cache_get(5, 3, 0)["team_size"] == 64
+    G.tuning_cache_clear()
