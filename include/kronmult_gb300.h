@@ -86,7 +86,9 @@ int kronmult_batched_f32_async(int matrix_count, int matrix_size, const float *c
 
 /*
  * Reduced-precision forward: FP32 factors and inputs, contraction in `compute`
- * (KRONMULT_COMPUTE_*), FP64 outputs accumulated with FP64 atomics.  Same
+ * (KRONMULT_COMPUTE_*), FP64 outputs accumulated with FP64 atomics.  TF32 and
+ * BF16 run the mode products on the tensor cores (tcgen05) and cover n == 8 with
+ * n^d <= 4096 (cudaErrorNotSupported otherwise); FP32 covers every shape.  Same
  * semantics as kronmult_batched otherwise (reference: kronmult_gpu/kronmult.cu:216-224
  * is the FP32 path; the FP64 output accumulation has no reference counterpart).
  */
@@ -159,6 +161,11 @@ int kronmult_tuning_cache_set(int matrix_count, int matrix_size, int dtype, cons
 int kronmult_tuning_cache_clear(void);
 int kronmult_tuning_cache_save(const char *path);
 int kronmult_tuning_cache_load(const char *path);
+
+/* Reads (and with clear != 0 resets) the device error word of the tensor-core
+ * kernels: 0 = no error; 1 = a bounded wait on an mbarrier timed out and the
+ * kernel left early (its outputs are then incomplete).  No reference counterpart. */
+int kronmult_device_error(int *code, int clear);
 
 /* Diagnostic: measured FP64 FMA throughput of the current GPU in GFLOP/s (no
  * reference counterpart).  Allocates and synchronises; not for use in a graph. */

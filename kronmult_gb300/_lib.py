@@ -72,6 +72,7 @@ SIGNATURES = {
     "kronmult_tuning_cache_clear": (_i, []),
     "kronmult_tuning_cache_save": (_i, [ctypes.c_char_p]),
     "kronmult_tuning_cache_load": (_i, [ctypes.c_char_p]),
+    "kronmult_device_error": (_i, [ctypes.POINTER(ctypes.c_int), _i]),
     "kronmult_diag_fp64_fma_gflops": (_i, [ctypes.POINTER(ctypes.c_double)]),
     "kronmult_pow_int": (ctypes.c_longlong, [_i, _i]),
     "kronmult_error_string": (ctypes.c_char_p, [_i]),

@@ -24,7 +24,8 @@ const DeviceInfo &device_info(int dev)
 
 bool ensure_smem_attr(const void *fn, size_t smem)
 {
-    if (smem <= 48 * 1024) return true;
+    // always raised explicitly (cached): a kernel's static shared memory also counts
+    // against the 48 KB default, so "dynamic <= 48 KB" alone is not safe
     static std::mutex mu;
     static std::map<std::pair<int, const void *>, size_t> done;
     int dev = 0;
@@ -62,6 +63,9 @@ int occupancy(const void *fn, int block, size_t smem)
     cache[key] = nblk;
     return nblk;
 }
+
+int launch_tc_forward(int kind, int d, int n, const float *const *mats, int stride, const float *const *in,
+                      double *const *out, long long nb, cudaStream_t st, const kronmult_tuning *tune);
 
 template <typename T, typename TO>
 static int forward_async(int d, int n, const T *const *mats, int stride, const T *const *in, TO *const *out,
@@ -219,7 +223,15 @@ int kronmult_batched_f32_f64out_async(int matrix_count, int matrix_size, const f
                                       double *const *output_batched, float *const *workspace_batched,
                                       int nb_batch, int compute, void *stream, const kronmult_tuning *tuning)
 {
-    if (compute != KRONMULT_COMPUTE_FP32) return cudaErrorNotSupported;
+    if (compute == KRONMULT_COMPUTE_TF32 || compute == KRONMULT_COMPUTE_BF16) {
+        if (matrix_count < 0 || matrix_size < 0 || nb_batch < 0 || matrix_stride < (matrix_size > 0 ? matrix_size : 1))
+            return cudaErrorInvalidValue;
+        if (nb_batch == 0) return cudaSuccess;
+        if (!matrix_list_batched || !input_batched || !output_batched) return cudaErrorInvalidValue;
+        return launch_tc_forward(compute, matrix_count, matrix_size, matrix_list_batched, matrix_stride,
+                                 input_batched, output_batched, nb_batch, (cudaStream_t)stream, tuning);
+    }
+    if (compute != KRONMULT_COMPUTE_FP32) return cudaErrorInvalidValue;
     return forward_async<float, double>(matrix_count, matrix_size, matrix_list_batched, matrix_stride,
                                         input_batched, output_batched, workspace_batched, nb_batch,
                                         (cudaStream_t)stream, tuning);

@@ -1,0 +1,364 @@
+// Tensor-core (tcgen05) forward for n = 8: FP32 storage, TF32 or BF16 mode
+// products with FP32 accumulation in tensor memory, FP64 output accumulation.
+//
+// For n = 8 every mode product of the backward sweep (kronmult_gpu/kronmult.cu:54-78)
+//     Y[c + r*F] = sum_k A_i(r, k) X[k + 8c],   F = N/8 fibres
+// is a dense GEMM D[c][r] = sum_k X^T[c][k] A_i^T[k][r] with M = F, N = 8, K = 8.
+// It runs as tcgen05.mma.cta_group::1 with M = 128 fibres per instruction
+// (N padded to 16, the smallest N for M = 128; K = 8 for TF32, K = 16 for BF16
+// with the upper 8 zero).  Operands live in shared memory in the canonical
+// K-major, no-swizzle layout of 8-row x 16-byte core matrices; the accumulator
+// lives in tensor memory, one 16-column block per 128-fibre tile.  After each
+// mode the four warps read their 32 TMEM lanes (tcgen05.ld.32x32b), round to the
+// operand type and write the mode output straight into the next mode's operand
+// layout at the rotated positions, so the vector never leaves shared memory.
+//
+// One CTA = one warpgroup (128 threads) works on one entry at a time; several
+// CTAs per SM overlap the input loads.  Consecutive entries with the same
+// output pointer are summed in FP64 registers and added with FP64 atomics.
+//
+// Every wait on an mbarrier is bounded; on timeout the kernel records an error
+// code in a device word (kronmult_device_error) and leaves after freeing its
+// tensor memory.
+#include <cuda_bf16.h>
+#include <cstdint>
+#include "fwd_launch.cuh"
+
+namespace kgb {
+
+__device__ unsigned int g_tc_error = 0;  // 0 = ok; otherwise the code of the first failure
+
+namespace {
+
+constexpr int kTcThreads = 128;
+constexpr int kTileRows = 128;               // fibres per MMA (M)
+constexpr int kTileBytes = kTileRows * 32;   // one K-major tile: 128 rows x 32 bytes
+constexpr int kBBytes = 16 * 32;             // one factor operand: 16 rows x 32 bytes
+constexpr unsigned kWaitLimit = 1u << 22;    // bounded mbarrier polling
+
+enum : int { KIND_TF32 = 0, KIND_BF16 = 1 };
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// byte offset of element (row, k) of a 32-byte-row K-major operand in core-matrix layout:
+// core matrix = 8 rows x 16 bytes (128 B contiguous); K-adjacent core matrices are
+// 128 B apart (leading byte offset), M-adjacent 8-row groups 256 B apart (stride byte offset)
+__device__ __forceinline__ uint32_t core_offset(uint32_t row, uint32_t kbyte)
+{
+    return (row >> 3) * 256u + (kbyte >> 4) * 128u + (row & 7u) * 16u + (kbyte & 15u);
+}
+
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);          // start address
+    d |= (uint64_t)((128u >> 4) & 0x3FFFu) << 16;     // leading byte offset (K direction)
+    d |= (uint64_t)((256u >> 4) & 0x3FFFu) << 32;     // stride byte offset (M/N direction)
+    d |= (uint64_t)1u << 46;                          // descriptor version for sm_100 family
+    return d;                                         // base offset 0, no swizzle
+}
+
+template <int KIND> __device__ __forceinline__ constexpr uint32_t instr_desc()
+{
+    // D = F32; A, B = TF32 (2) or BF16 (1); both K-major; N = 16; M = 128
+    return (1u << 4) | ((KIND == KIND_TF32 ? 2u : 1u) << 7) | ((KIND == KIND_TF32 ? 2u : 1u) << 10) |
+           ((16u >> 3) << 17) | ((128u >> 4) << 24);
+}
+
+template <int KIND>
+__device__ __forceinline__ void mma(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate)
+{
+    if constexpr (KIND == KIND_TF32) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
+            "l"(adesc), "l"(bdesc), "r"(instr_desc<KIND>()), "r"(accumulate));
+    } else {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
+            "l"(adesc), "l"(bdesc), "r"(instr_desc<KIND>()), "r"(accumulate));
+    }
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t mbar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase)
+{
+    for (unsigned it = 0; it < kWaitLimit; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.b32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(phase)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8])
+{
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ float to_tf32(float x)
+{
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
+// store one value of the operand element (row, k) in the operand type of KIND
+template <int KIND> __device__ __forceinline__ void put(unsigned char *base, uint32_t row, uint32_t k, float v)
+{
+    if constexpr (KIND == KIND_TF32) {
+        *reinterpret_cast<float *>(base + core_offset(row, k * 4u)) = to_tf32(v);
+    } else {
+        *reinterpret_cast<__nv_bfloat16 *>(base + core_offset(row, k * 2u)) = __float2bfloat16_rn(v);
+    }
+}
+
+}  // namespace
+
+struct TcArgs {
+    const float *const *mats;
+    const float *const *in;
+    double *const *out;
+    long long nb;
+    int d, stride, N, tiles, tmem_cols, entries_per_cta;
+};
+
+template <int KIND> __global__ void __launch_bounds__(kTcThreads) fwd_tc_kernel(const TcArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    unsigned char *xs = smem_raw;                                 // tiles x 4 KB operand A
+    unsigned char *bs = xs + (size_t)a.tiles * kTileBytes;        // d x 512 B operand B
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(bs + (size_t)a.d * kBBytes);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int N = a.N, F = N / 8, d = a.d;
+
+    long long e = (long long)blockIdx.x * a.entries_per_cta;
+    const long long e_end = min(e + (long long)a.entries_per_cta, a.nb);
+    if (e >= e_end) return;
+
+    // zero both operands once: padding rows of B (8..15) and, for BF16, the K 8..15 half of A stay zero
+    for (int v = tid; v < (a.tiles * kTileBytes + d * kBBytes) / 16; v += kTcThreads)
+        reinterpret_cast<int4 *>(smem_raw)[v] = make_int4(0, 0, 0, 0);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(a.tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t mbar_a = smem_u32(mbar);
+    const uint32_t xs_a = smem_u32(xs), bs_a = smem_u32(bs);
+    uint32_t phase = 0;
+    bool failed = false;
+
+    constexpr int MAXT = 4;  // tiles per entry held in registers (N <= 4096)
+    double acc[MAXT][8];
+    double *cur = nullptr;
+
+    for (; e < e_end && !failed; ++e) {
+        const float *x = a.in[e];
+        double *o = a.out[e];
+        // factors: B_i[row r][k] = A_i(r, k), rows 8..15 stay zero
+        const float *const *mats = a.mats + e * d;
+        for (int v = tid; v < d * 64; v += kTcThreads) {
+            const int i = v >> 6, r = (v >> 3) & 7, k = v & 7;
+            put<KIND>(bs + (size_t)i * kBBytes, r, k, mats[i][r + (size_t)k * a.stride]);
+        }
+        // input: natural index p = k + 8c -> operand row c, column k
+        if ((reinterpret_cast<uintptr_t>(x) & 15u) == 0) {
+            for (int q = tid; q < N / 4; q += kTcThreads) {
+                const float4 v4 = __ldcs(reinterpret_cast<const float4 *>(x) + q);
+                const uint32_t c = q >> 1, k0 = (q & 1) * 4;
+                put<KIND>(xs, c, k0 + 0, v4.x);
+                put<KIND>(xs, c, k0 + 1, v4.y);
+                put<KIND>(xs, c, k0 + 2, v4.z);
+                put<KIND>(xs, c, k0 + 3, v4.w);
+            }
+        } else {
+            for (int p = tid; p < N; p += kTcThreads) put<KIND>(xs, p >> 3, p & 7, __ldcs(x + p));
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+
+        float v[MAXT][8];
+        for (int i = d - 1; i >= 0; --i) {
+            if (tid == 0) {
+                tc_fence_after();
+                for (int t = 0; t < a.tiles; ++t)
+                    mma<KIND>(tmem + 16u * t, smem_desc(xs_a + t * kTileBytes), smem_desc(bs_a + i * kBBytes), 0u);
+                mma_commit(mbar_a);
+            }
+            const bool ok = mbar_wait(mbar_a, phase);
+            // the decision to leave must be uniform: the TMEM loads below are warp-collective
+            if (__syncthreads_or(!ok)) {
+                if (tid == 0) atomicCAS(&g_tc_error, 0u, 1u);
+                failed = true;
+                break;
+            }
+            phase ^= 1u;
+            tc_fence_after();
+#pragma unroll
+            for (int t = 0; t < MAXT; ++t)
+                if (t < a.tiles) tmem_ld8(tmem + ((uint32_t)(warp * 32) << 16) + 16u * t, v[t]);
+            tmem_wait_ld();
+            if (i > 0) {
+                // mode output element (row c, r) goes to natural position p = c + r*F,
+                // which is operand row p/8, column p%8 of the next mode
+#pragma unroll
+                for (int t = 0; t < MAXT; ++t) {
+                    const int c = t * kTileRows + warp * 32 + lane;
+                    if (t < a.tiles && c < F) {
+#pragma unroll
+                        for (int r = 0; r < 8; ++r) {
+                            const uint32_t p = c + r * F;
+                            put<KIND>(xs, p >> 3, p & 7, v[t][r]);
+                        }
+                    }
+                }
+                fence_async_smem();
+            }
+            tc_fence_before();
+            __syncthreads();
+        }
+        if (failed) break;
+        // v[t][r] is element c + r*F of kron(A) . x
+        if (o != cur) {
+            if (cur != nullptr) {
+#pragma unroll
+                for (int t = 0; t < MAXT; ++t) {
+                    const int c = t * kTileRows + warp * 32 + lane;
+                    if (t < a.tiles && c < F)
+#pragma unroll
+                        for (int r = 0; r < 8; ++r) atomicAdd(cur + c + r * F, acc[t][r]);
+                }
+            }
+            cur = o;
+#pragma unroll
+            for (int t = 0; t < MAXT; ++t)
+#pragma unroll
+                for (int r = 0; r < 8; ++r) acc[t][r] = (double)v[t][r];
+        } else {
+#pragma unroll
+            for (int t = 0; t < MAXT; ++t)
+#pragma unroll
+                for (int r = 0; r < 8; ++r) acc[t][r] += (double)v[t][r];
+        }
+    }
+    if (cur != nullptr && !failed) {
+#pragma unroll
+        for (int t = 0; t < MAXT; ++t) {
+            const int c = t * kTileRows + warp * 32 + lane;
+            if (t < a.tiles && c < F)
+#pragma unroll
+                for (int r = 0; r < 8; ++r) atomicAdd(cur + c + r * F, acc[t][r]);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(a.tmem_cols) : "memory");
+}
+
+// Plans and enqueues the tensor-core forward.  Returns cudaErrorNotSupported for
+// shapes it does not cover (n != 8, n^d > 4096), so that the caller can fall back.
+int launch_tc_forward(int kind, int d, int n, const float *const *mats, int stride, const float *const *in,
+                      double *const *out, long long nb, cudaStream_t st, const kronmult_tuning *tune)
+{
+    if (n != 8 || d < 1) return cudaErrorNotSupported;
+    const long long Nl = pow_ll(n, d);
+    if (Nl > 4096) return cudaErrorNotSupported;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return cudaErrorInvalidDevice;
+    const DeviceInfo &di = device_info(dev);
+    TcArgs a{};
+    a.mats = mats;
+    a.in = in;
+    a.out = out;
+    a.nb = nb;
+    a.d = d;
+    a.stride = stride;
+    a.N = (int)Nl;
+    const int F = a.N / 8;
+    a.tiles = (F + kTileRows - 1) / kTileRows;
+    int cols = 32;
+    while (cols < 16 * a.tiles) cols *= 2;
+    a.tmem_cols = cols;
+    const size_t need = (size_t)a.tiles * kTileBytes + (size_t)d * kBBytes + 16;
+    // resident CTAs per SM are limited so that their tensor-memory columns fit in 512:
+    // each CTA reserves at least 1/max_ctas of the SM's shared memory
+    const int max_ctas = 512 / cols;
+    size_t smem = need;
+    const size_t per_sm = 228 * 1024;
+    if (smem * max_ctas < per_sm) smem = per_sm / max_ctas - 1024 + 16;
+    if (smem < need) smem = need;
+    if (smem > (size_t)di.max_smem_optin) return cudaErrorNotSupported;
+    const void *fn = kind == KRONMULT_COMPUTE_TF32 ? (const void *)fwd_tc_kernel<KIND_TF32>
+                                                   : (const void *)fwd_tc_kernel<KIND_BF16>;
+    if (!ensure_smem_attr(fn, smem)) return cudaErrorInvalidValue;
+    int occ = occupancy(fn, kTcThreads, smem);
+    if (occ < 1) return cudaErrorNotSupported;
+    if (occ > max_ctas) occ = max_ctas;
+    if (tune && tune->ctas_per_sm > 0 && tune->ctas_per_sm < occ) occ = tune->ctas_per_sm;
+    const long long ctas = (long long)di.sms * occ;
+    long long ept = (tune && tune->entries_per_team > 0) ? tune->entries_per_team : (nb + ctas - 1) / ctas;
+    if (ept < 1) ept = 1;
+    if (ept > INT_MAX) ept = INT_MAX;
+    a.entries_per_cta = (int)ept;
+    const long long grid = (nb + ept - 1) / ept;
+    if (grid > INT_MAX) return cudaErrorInvalidValue;
+    if (kind == KRONMULT_COMPUTE_TF32)
+        fwd_tc_kernel<KIND_TF32><<<(unsigned)grid, kTcThreads, smem, st>>>(a);
+    else
+        fwd_tc_kernel<KIND_BF16><<<(unsigned)grid, kTcThreads, smem, st>>>(a);
+    return (int)cudaGetLastError();
+}
+
+}  // namespace kgb
+
+extern "C" int kronmult_device_error(int *code, int clear)
+{
+    if (!code) return cudaErrorInvalidValue;
+    unsigned v = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(&v, kgb::g_tc_error, sizeof v);
+    if (e != cudaSuccess) return e;
+    *code = (int)v;
+    if (clear && v) {
+        const unsigned z = 0;
+        e = cudaMemcpyToSymbol(kgb::g_tc_error, &z, sizeof z);
+    }
+    return e;
+}

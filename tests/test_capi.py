@@ -120,3 +120,28 @@ def test_tuning_cache_roundtrip_on_host(lib, tmp_path):
     G.tuning_cache_load(path)
     assert G.tuning_cache_get(5, 3, 0)["team_size"] == 64
     G.tuning_cache_clear()
+
+
+def build_drop_in(tmp_dir):
+    """Compile tests/cpp/drop_in.cpp, a caller written against the reference's
+    kronmult.cuh interface, against include/kronmult.cuh and the library."""
+    import shutil
+    import subprocess
+
+    from kronmult_gb300 import _lib
+
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    cuda_home = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    exe = os.path.join(str(tmp_dir), "drop_in")
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    cmd = [cxx, "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), "-I", os.path.join(cuda_home, "include"),
+           os.path.join(ROOT, "tests", "cpp", "drop_in.cpp"), "-o", exe, "-L", libdir, "-lkronmult_gb300",
+           "-L", os.path.join(cuda_home, "lib64"), "-lcudart", f"-Wl,-rpath,{libdir}"]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+    return exe
+
+
+def test_cpp_drop_in_compiles(lib, tmp_path):
+    assert os.path.exists(build_drop_in(tmp_path))

@@ -180,3 +180,14 @@ def test_linearity_full_config4_f32(cuda):
     torch.cuda.synchronize()
     # the atomic order may differ between the runs; compare normwise
     assert (torch.linalg.norm(db.outputs - 2 * y1) / torch.linalg.norm(2 * y1)).item() <= 1e-14
+
+
+def test_cpp_drop_in_runs(cuda, tmp_path):
+    """The reference-style C++ caller, linked against the library, passes its own check."""
+    import subprocess
+
+    from test_capi import build_drop_in
+
+    exe = build_drop_in(tmp_path)
+    p = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert p.returncode == 0, p.stdout + p.stderr

@@ -1,0 +1,95 @@
+"""Tensor-core (tcgen05) reduced-precision forward for n = 8: TF32 and BF16 mode
+products with FP32 accumulation and FP64 output accumulation, against the FP64
+oracle.  Errors are stated against FP64 (relative L2):
+  FP32 CUDA-core  <= 1e-6   TF32 tensor core  <= 2e-3   BF16 tensor core  <= 2e-2
+(TF32 keeps 10 mantissa bits, BF16 7; each of the d roundings of the vector and
+of the factors contributes about 2^-11 resp. 2^-8 relative error.)"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"fp32": 1e-6, "tf32": 2e-3, "bf16": 2e-2}
+
+
+def run_mode(b, cuda, compute):
+    from kronmult_gb300 import DeviceBatch, _lib, forward_f32_f64out
+
+    code = {"fp32": _lib.KRONMULT_COMPUTE_FP32, "tf32": _lib.KRONMULT_COMPUTE_TF32,
+            "bf16": _lib.KRONMULT_COMPUTE_BF16}[compute]
+    db = DeviceBatch.from_host(b, device=cuda, dtype=torch.float32, out_dtype=torch.float64)
+    forward_f32_f64out(db, compute=code)
+    torch.cuda.synchronize()
+    err = ctypes_device_error()
+    assert err == 0, f"device error word {err}"
+    return db.outputs.cpu().numpy()
+
+
+def ctypes_device_error():
+    import ctypes
+
+    from kronmult_gb300 import _lib
+
+    c = ctypes.c_int(0)
+    _lib.check(_lib.lib().kronmult_device_error(ctypes.byref(c), 1), "kronmult_device_error")
+    return c.value
+
+
+@pytest.mark.parametrize("compute", ["tf32", "bf16"])
+@pytest.mark.parametrize("d", [1, 2, 3, 4])
+def test_tc_shapes(cuda, compute, d):
+    from kronmult_gb300 import workloads as W
+
+    b = W.make_batch(d, 8, 8, 5, 3, seed=40 + d, factor_scale=1 / 8)
+    got = run_mode(b, cuda, compute)
+    assert O.rel_l2(got, O.forward(b)) <= TOL[compute]
+
+
+@pytest.mark.parametrize("compute", ["fp32", "tf32", "bf16"])
+def test_config4_sample(cuda, compute):
+    from kronmult_gb300 import workloads as W
+
+    b = W.config4(scale=32 / 4096)
+    got = run_mode(b, cuda, compute)
+    err = O.rel_l2(got, O.forward(b))
+    assert err <= TOL[compute]
+
+
+def test_tc_matches_tf32_rounded_oracle(cuda):
+    """The TF32 path equals an FP32 sweep whose operands are rounded to TF32 before
+    every mode (round-to-nearest-even at 10 mantissa bits), up to FP32 summation order."""
+    from kronmult_gb300 import workloads as W
+
+    b = W.make_batch(2, 8, 8, 3, 2, seed=77, factor_scale=1 / 8)
+    got = run_mode(b, cuda, "tf32")
+
+    def tf32(a):
+        a = np.asarray(a, dtype=np.float32).view(np.uint32).astype(np.uint64)
+        r = ((a + 0x1000) & ~np.uint64(0x1FFF)).astype(np.uint32)
+        return r.view(np.float32).astype(np.float64)
+
+    out = b.out_init.copy()
+    for k in range(b.nb):
+        x = tf32(b.inputs[k].astype(np.float32))
+        for i in range(b.d - 1, -1, -1):
+            A = b.factors[b.fac_index[k] * b.d + i]
+            M = tf32(np.array([[A[r + c * b.stride] for c in range(8)] for r in range(8)], dtype=np.float32))
+            F = x.size // 8
+            y = (M @ x.reshape(F, 8).T).astype(np.float32)  # y[r, c]
+            x = y.reshape(-1).astype(np.float64)
+            if i > 0:
+                x = tf32(x)
+        out[b.out_index[k]] += x
+    assert O.rel_l2(got, out) <= 1e-5
+
+
+def test_tc_rejects_unsupported_shape(cuda):
+    import kronmult_gb300 as K
+    from kronmult_gb300 import workloads as W
+
+    b = W.make_batch(2, 4, 4, 2, 2, seed=1)
+    with pytest.raises(K.KronmultError):
+        run_mode(b, cuda, "tf32")
