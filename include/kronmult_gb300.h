@@ -55,6 +55,7 @@ typedef struct kronmult_tuning {
     int team_size;        /* threads cooperating on one entry: 8,16,...,512 */
     int ctas_per_sm;      /* resident CTAs per SM to size the grid for (0 = occupancy) */
     int entries_per_team; /* contiguous entries one team processes (0 = one wave) */
+    int prefetch;         /* 0 = automatic, 1 = one staging slot, 2 = copy the next entry asynchronously */
 } kronmult_tuning;
 
 /*

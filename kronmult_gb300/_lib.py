@@ -19,7 +19,8 @@ KRONMULT_COMPUTE_BF16 = 2
 class Tuning(ctypes.Structure):
     """Mirror of `kronmult_tuning`: launch-shape override, zero = heuristic."""
 
-    _fields_ = [("team_size", ctypes.c_int), ("ctas_per_sm", ctypes.c_int), ("entries_per_team", ctypes.c_int)]
+    _fields_ = [("team_size", ctypes.c_int), ("ctas_per_sm", ctypes.c_int), ("entries_per_team", ctypes.c_int),
+                ("prefetch", ctypes.c_int)]
 
 
 class Group(ctypes.Structure):
@@ -117,5 +118,6 @@ def tuning_ptr(t: Tuning | dict | None):
     if t is None:
         return None
     if isinstance(t, dict):
-        t = Tuning(int(t.get("team_size", 0)), int(t.get("ctas_per_sm", 0)), int(t.get("entries_per_team", 0)))
+        t = Tuning(int(t.get("team_size", 0)), int(t.get("ctas_per_sm", 0)), int(t.get("entries_per_team", 0)),
+                   int(t.get("prefetch", 0)))
     return ctypes.byref(t)

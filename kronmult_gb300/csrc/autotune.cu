@@ -93,8 +93,9 @@ int autotune_impl(int d, int n, int dtype, int nb_sample, kronmult_tuning *best,
             const int q = (F + ts - 1) / ts;
             if (q > qcap) continue;
             if (ts > 8 && (F + ts / 2 - 1) / (ts / 2) == 1 && ts > F) continue;  // larger teams only idle
-            for (int ept : {0, 2, 8}) {
-                kronmult_tuning t{ts, 0, ept};
+            for (int cand = 0; cand < 6; ++cand) {
+                const int ept = (cand % 3 == 0) ? 0 : (cand % 3 == 1 ? 2 : 8);
+                kronmult_tuning t{ts, 0, ept, cand < 3 ? 2 : 1};
                 FwdPlan<T, TO> pl;
                 if (plan_forward<T, TO>(pl, d, n, mats, n, in, out, nullptr, nb, &t) != cudaSuccess) continue;
                 if (!pl.smem_path) continue;
@@ -183,7 +184,8 @@ int kronmult_tuning_cache_get(int matrix_count, int matrix_size, int dtype, kron
 
 int kronmult_tuning_cache_set(int matrix_count, int matrix_size, int dtype, const kronmult_tuning *t)
 {
-    if (!t || t->team_size < 0 || t->ctas_per_sm < 0 || t->entries_per_team < 0) return cudaErrorInvalidValue;
+    if (!t || t->team_size < 0 || t->ctas_per_sm < 0 || t->entries_per_team < 0 || t->prefetch < 0 || t->prefetch > 2)
+        return cudaErrorInvalidValue;
     tuning_cache_store(matrix_count, matrix_size, dtype, *t);
     return cudaSuccess;
 }
@@ -201,10 +203,11 @@ int kronmult_tuning_cache_save(const char *path)
     FILE *f = std::fopen(path, "w");
     if (!f) return cudaErrorInvalidValue;
     std::lock_guard<std::mutex> lk(g_mu);
-    std::fprintf(f, "# kronmult_gb300 tuning cache v1: sms d n dtype team_size ctas_per_sm entries_per_team\n");
+    std::fprintf(f, "# kronmult_gb300 tuning cache v2: sms d n dtype team_size ctas_per_sm entries_per_team prefetch\n");
     for (auto &kv : g_cache)
-        std::fprintf(f, "%d %d %d %d %d %d %d\n", std::get<0>(kv.first), std::get<1>(kv.first), std::get<2>(kv.first),
-                     std::get<3>(kv.first), kv.second.team_size, kv.second.ctas_per_sm, kv.second.entries_per_team);
+        std::fprintf(f, "%d %d %d %d %d %d %d %d\n", std::get<0>(kv.first), std::get<1>(kv.first), std::get<2>(kv.first),
+                     std::get<3>(kv.first), kv.second.team_size, kv.second.ctas_per_sm, kv.second.entries_per_team,
+                     kv.second.prefetch);
     std::fclose(f);
     return cudaSuccess;
 }
@@ -218,9 +221,11 @@ int kronmult_tuning_cache_load(const char *path)
     std::lock_guard<std::mutex> lk(g_mu);
     while (std::fgets(line, sizeof line, f)) {
         if (line[0] == '#') continue;
-        int v[7];
-        if (std::sscanf(line, "%d %d %d %d %d %d %d", &v[0], &v[1], &v[2], &v[3], &v[4], &v[5], &v[6]) == 7)
-            g_cache[std::make_tuple(v[0], v[1], v[2], v[3])] = kronmult_tuning{v[4], v[5], v[6]};
+        int v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        const int got = std::sscanf(line, "%d %d %d %d %d %d %d %d", &v[0], &v[1], &v[2], &v[3], &v[4], &v[5], &v[6],
+                                    &v[7]);
+        if (got == 7 || got == 8)
+            g_cache[std::make_tuple(v[0], v[1], v[2], v[3])] = kronmult_tuning{v[4], v[5], v[6], v[7]};
     }
     std::fclose(f);
     return cudaSuccess;

@@ -31,6 +31,8 @@ template <typename T, typename TO> struct FwdArgs {
     int entries_per_team;  // contiguous entries each team processes
     int team_elems;        // shared-memory elements reserved per team
     int vec_pad;           // offset of the factor area inside a team's slice (elements)
+    int fac_pad;           // padded size of the factor area (elements)
+    int prefetch;          // 1: two staging slots per team, next entry copied asynchronously
 };
 
 // ---- helpers ---------------------------------------------------------------
@@ -98,6 +100,45 @@ template <typename T, int NN> __device__ __forceinline__ void load_fibre(const T
 template <typename T> __device__ __forceinline__ T fma_t(T a, T b, T c) { return fma(a, b, c); }
 template <> __device__ __forceinline__ float fma_t<float>(float a, float b, float c) { return fmaf(a, b, c); }
 
+// ---- asynchronous global->shared copies (cp.async, completion per thread) --
+
+template <int BYTES> __device__ __forceinline__ void cp_async(void *dst, const void *src)
+{
+    const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+    if constexpr (BYTES == 16) {
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+    } else {
+        asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(d), "l"(src), "n"(BYTES) : "memory");
+    }
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// issue the copies of one entry's input vector and factors into a staging slot
+// (same layouts as stage_vector / stage_factors); completes with cp_async_wait_all
+template <typename T, int NN>
+__device__ __forceinline__ void stage_async(T *dst, T *fac, const T *src, const T *const *mats, int N, int d,
+                                            int stride, const Team &tm)
+{
+    const size_t bytes = (size_t)N * sizeof(T);
+    if (((reinterpret_cast<uintptr_t>(src) & 15u) == 0) && ((bytes & 15u) == 0)) {
+        const int nv = (int)(bytes >> 4);
+        for (int v = tm.rank; v < nv; v += tm.size)
+            cp_async<16>(reinterpret_cast<int4 *>(dst) + v, reinterpret_cast<const int4 *>(src) + v);
+    } else {
+        for (int v = tm.rank; v < N; v += tm.size) cp_async<(int)sizeof(T)>(dst + v, src + v);
+    }
+    constexpr int NN2 = NN * NN;
+    for (int idx = tm.rank; idx < d * NN2; idx += tm.size) {
+        const int i = idx / NN2;
+        const int rem = idx - i * NN2;
+        const int k = rem / NN;
+        const int r = rem - k * NN;
+        cp_async<(int)sizeof(T)>(fac + idx, mats[i] + r + (size_t)k * stride);
+    }
+    cp_async_commit();
+}
+
 // ---- shared-memory, register in-place team forward (compile-time n) -------
 //
 // Thread `rank` of a team owns fibres c = rank + q*team_size (q < QMAX) in every
@@ -111,11 +152,14 @@ template <> __device__ __forceinline__ float fma_t<float>(float a, float b, floa
 // flushed with atomic adds, or -- in deterministic mode, where the caller
 // guarantees that every output pointer is one contiguous run owned by this team --
 // with a plain read-modify-write, so that the sum order is the entry order.
-template <typename T, typename TO, int NN, int QMAX, bool DET>
+template <typename T, typename TO, int NN, int QMAX, bool DET, bool PF = false>
 __device__ __forceinline__ void team_forward(const T *const *mats, const T *const *in, TO *const *out,
                                              const long long *perm, int d, int stride, int N, long long e_begin,
-                                             long long e_end, T *buf, T *fac, const Team &tm)
+                                             long long e_end, T *buf, T *fac, const Team &tm, T *buf2 = nullptr,
+                                             T *fac2 = nullptr)
 {
+    // PF: two staging slots (buf/fac and buf2/fac2); the copies of entry e+1 are in
+    // flight (cp.async) while entry e is computed
     const int F = N / NN;
     TO acc[QMAX][NN];
     TO *cur = nullptr;
@@ -137,13 +181,27 @@ __device__ __forceinline__ void team_forward(const T *const *mats, const T *cons
         }
     };
 
+    if constexpr (PF) {
+        if (e_begin < e_end) {
+            const long long e0 = perm ? perm[e_begin] : e_begin;
+            stage_async<T, NN>(buf, fac, in[e0], mats + e0 * d, N, d, stride, tm);
+        }
+    }
     for (long long ei = e_begin; ei < e_end; ++ei) {
         const long long e = perm ? perm[ei] : ei;
-        const T *x = in[e];
         TO *o = out[e];
-        stage_vector(buf, x, N, tm);
-        stage_factors<T, NN>(fac, mats + e * d, d, stride, tm);
-        tm.sync();
+        if constexpr (PF) {
+            cp_async_wait_all();
+            tm.sync();  // slot of entry e complete for the whole team
+            if (ei + 1 < e_end) {
+                const long long en = perm ? perm[ei + 1] : ei + 1;
+                stage_async<T, NN>(buf2, fac2, in[en], mats + en * d, N, d, stride, tm);
+            }
+        } else {
+            stage_vector(buf, in[e], N, tm);
+            stage_factors<T, NN>(fac, mats + e * d, d, stride, tm);
+            tm.sync();
+        }
 
         T y[QMAX][NN];
         for (int i = d - 1; i >= 0; --i) {
@@ -201,6 +259,14 @@ __device__ __forceinline__ void team_forward(const T *const *mats, const T *cons
 #pragma unroll
                 for (int r = 0; r < NN; ++r) acc[q][r] += (TO)y[q][r];
         }
+        if constexpr (PF) {
+            T *t = buf;
+            buf = buf2;
+            buf2 = t;
+            t = fac;
+            fac = fac2;
+            fac2 = t;
+        }
     }
     if (cur != nullptr) flush(cur);
 }
@@ -215,7 +281,15 @@ __global__ void __launch_bounds__(512) fwd_smem_kernel(const FwdArgs<T, TO> a)
     const long long team_global = (long long)blockIdx.x * a.teams_per_cta + tm.id;
     const long long e = team_global * a.entries_per_team;
     const long long e_end = min(e + (long long)a.entries_per_team, a.nb);
-    team_forward<T, TO, NN, QMAX, false>(a.mats, a.in, a.out, nullptr, a.d, a.stride, a.N, e, e_end, buf, fac, tm);
+    if (a.prefetch) {
+        T *buf2 = fac + a.fac_pad;
+        T *fac2 = buf2 + a.vec_pad;
+        team_forward<T, TO, NN, QMAX, false, true>(a.mats, a.in, a.out, nullptr, a.d, a.stride, a.N, e, e_end, buf,
+                                                   fac, tm, buf2, fac2);
+    } else {
+        team_forward<T, TO, NN, QMAX, false>(a.mats, a.in, a.out, nullptr, a.d, a.stride, a.N, e, e_end, buf, fac,
+                                             tm);
+    }
 }
 
 // ---- generic kernel (runtime n, any N) ------------------------------------

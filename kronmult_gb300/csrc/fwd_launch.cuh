@@ -108,7 +108,12 @@ int plan_forward(FwdPlan<T, TO> &pl, int d, int n, const T *const *mats, int str
         const bool ts_ok = (ts == 8 || ts == 16 || ts == 32 || ts == 64 || ts == 128 || ts == 256 || ts == 512);
         if (ts_ok && qmax <= qcap) {
             const int vpad = round_up(N, 16 / (int)sizeof(T));
-            const int team_elems = vpad + round_up(d * n * n, 16 / (int)sizeof(T));
+            const int fpad = round_up(d * n * n, 16 / (int)sizeof(T));
+            // two staging slots (asynchronous prefetch of the next entry) unless disabled
+            // or too large for a quarter of the SM's shared memory
+            int prefetch = (tune && tune->prefetch == 1) ? 0 : 1;
+            if ((size_t)2 * (vpad + fpad) * sizeof(T) > (size_t)di.max_smem_optin / 2) prefetch = 0;
+            const int team_elems = (prefetch ? 2 : 1) * (vpad + fpad);
             const size_t team_bytes = (size_t)team_elems * sizeof(T);
             int block = ts >= 256 ? ts : 256;
             int teams = block / ts;
@@ -142,6 +147,8 @@ int plan_forward(FwdPlan<T, TO> &pl, int d, int n, const T *const *mats, int str
                         a.entries_per_team = (int)ept;
                         a.team_elems = team_elems;
                         a.vec_pad = vpad;
+                        a.fac_pad = fpad;
+                        a.prefetch = prefetch;
                         pl.fn = (const void *)fn;
                         pl.smem_path = true;
                         pl.grid = dim3((unsigned)grid);

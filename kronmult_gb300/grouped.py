@@ -48,6 +48,7 @@ class GroupedPlan:
                 a.team_size = int(t.get("team_size", 0))
                 a.ctas_per_sm = int(t.get("ctas_per_sm", 0))
                 a.entries_per_team = int(t.get("entries_per_team", 0))
+                a.prefetch = int(t.get("prefetch", 0))
             tp = arr
         self._h = ctypes.c_void_p()
         st = _lib.lib().kronmult_grouped_plan_create(ctypes.byref(self._h), groups, len(batches), DTYPES[dt],
@@ -80,19 +81,24 @@ def autotune_forward(d: int, n: int, dtype: int = _lib.KRONMULT_DTYPE_F64, nb_sa
     ms = ctypes.c_float(0)
     _lib.check(_lib.lib().kronmult_autotune_forward(d, n, dtype, nb_sample, ctypes.byref(t), ctypes.byref(ms)),
                "kronmult_autotune_forward")
-    return {"team_size": t.team_size, "ctas_per_sm": t.ctas_per_sm, "entries_per_team": t.entries_per_team}, ms.value
+    return _as_dict(t), ms.value
 
 
 def tuning_cache_get(d: int, n: int, dtype: int = _lib.KRONMULT_DTYPE_F64):
     t = _lib.Tuning()
     if _lib.lib().kronmult_tuning_cache_get(d, n, dtype, ctypes.byref(t)) != 0:
         return None
-    return {"team_size": t.team_size, "ctas_per_sm": t.ctas_per_sm, "entries_per_team": t.entries_per_team}
+    return _as_dict(t)
+
+
+def _as_dict(t) -> dict:
+    return {"team_size": t.team_size, "ctas_per_sm": t.ctas_per_sm, "entries_per_team": t.entries_per_team,
+            "prefetch": t.prefetch}
 
 
 def tuning_cache_set(d: int, n: int, dtype: int, tuning: dict) -> None:
     t = _lib.Tuning(int(tuning.get("team_size", 0)), int(tuning.get("ctas_per_sm", 0)),
-                    int(tuning.get("entries_per_team", 0)))
+                    int(tuning.get("entries_per_team", 0)), int(tuning.get("prefetch", 0)))
     _lib.check(_lib.lib().kronmult_tuning_cache_set(d, n, dtype, ctypes.byref(t)), "kronmult_tuning_cache_set")
 
 

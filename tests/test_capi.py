@@ -112,7 +112,7 @@ def test_tuning_cache_roundtrip_on_host(lib, tmp_path):
 
     G.tuning_cache_clear()
     G.tuning_cache_set(5, 3, 0, {"team_size": 64, "entries_per_team": 4})
-    assert G.tuning_cache_get(5, 3, 0) == {"team_size": 64, "ctas_per_sm": 0, "entries_per_team": 4}
+    assert G.tuning_cache_get(5, 3, 0) == {"team_size": 64, "ctas_per_sm": 0, "entries_per_team": 4, "prefetch": 0}
     path = str(tmp_path / "t.txt")
     G.tuning_cache_save(path)
     G.tuning_cache_clear()

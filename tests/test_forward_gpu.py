@@ -87,14 +87,29 @@ def test_config5_shared_factors(cuda):
     assert O.rel_l2(got32, O.forward(b)) <= TOL32
 
 
+@pytest.mark.parametrize("prefetch", [1, 2])
 @pytest.mark.parametrize("team_size", [8, 16, 32, 64, 128, 256, 512])
-def test_team_sizes_agree(cuda, team_size):
+def test_team_sizes_agree(cuda, team_size, prefetch):
     """Every launch shape the autotuner may pick gives the oracle's result."""
     from kronmult_gb300 import workloads as W
 
     b = W.make_batch(5, 4, 5, 7, 6, seed=99)
-    got, _ = run(b, cuda, tuning={"team_size": team_size, "entries_per_team": 3})
+    got, _ = run(b, cuda, tuning={"team_size": team_size, "entries_per_team": 3, "prefetch": prefetch})
     assert O.rel_l2(got, O.forward(b)) <= TOL64
+
+
+@pytest.mark.parametrize("n", [2, 3, 5, 6, 7, 8])
+def test_prefetch_odd_sizes(cuda, n):
+    """Unaligned vector lengths take the element-wise asynchronous copy."""
+    from kronmult_gb300 import workloads as W
+
+    d = 3 if n <= 6 else 2
+    b = W.make_batch(d, n, n + 2, 4, 5, seed=200 + n)
+    for pf in (1, 2):
+        got, _ = run(b, cuda, tuning={"prefetch": pf, "entries_per_team": 4})
+        assert O.rel_l2(got, O.forward(b)) <= TOL64
+        got32, _ = run(b, cuda, dtype=torch.float32, tuning={"prefetch": pf, "entries_per_team": 4})
+        assert O.rel_l2(got32, O.forward(b)) <= TOL32
 
 
 def test_inputs_not_modified(cuda):
