@@ -163,6 +163,33 @@ int kronmult_tuning_cache_clear(void);
 int kronmult_tuning_cache_save(const char *path);
 int kronmult_tuning_cache_load(const char *path);
 
+/*
+ * Allocation-free FP64 forward (no counterpart in the reference).
+ *
+ * For callers that cannot call cudaMalloc where they run the product: code inside
+ * an application-owned memory pool or arena, allocator-free callbacks, runtimes
+ * that forbid device allocation after start-up.  The work list that the grouped
+ * forward keeps in plan-allocated device memory lives here in a fixed array
+ * compiled into the library (4 MiB + 256 bytes, held by every GPU that loads the
+ * library until the process exits), so a call allocates nothing.
+ *
+ * Same result as kronmult_batched_f64 (output[k] += kron(A_k) . input[k], atomic
+ * into shared outputs); inputs are not modified; every pointer array on the
+ * device.  Each run of consecutive entries with one output pointer is summed in
+ * entry order and added with one atomic per element, so the result is bitwise
+ * reproducible when every output's entries form one contiguous run.
+ * Limits: nb_batch <= KRONMULT_NOALLOC_MAX_ENTRIES (else cudaErrorInvalidValue),
+ * 2 <= matrix_size <= 8 with n^d fitting one team's shared memory (else
+ * cudaErrorNotSupported).  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress) with that device current; make that first
+ * call before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU (other streams, other host threads) race and must be serialised.
+ */
+#define KRONMULT_NOALLOC_MAX_ENTRIES 1048576
+int kronmult_batched_f64_noalloc(int matrix_count, int matrix_size, const double *const *matrix_list_batched,
+                                 int matrix_stride, const double *const *input_batched,
+                                 double *const *output_batched, int nb_batch, void *stream);
+
 /* Reads (and with clear != 0 resets) the device error word of the tensor-core
  * kernels: 0 = no error; 1 = a bounded wait on an mbarrier timed out and the
  * kernel left early (its outputs are then incomplete).  No reference counterpart. */

@@ -36,6 +36,7 @@ KRONMULT_DTYPE_F32 = 1
 KRONMULT_DTYPE_F32_F64OUT = 2
 KRONMULT_MODE_ATOMIC = 0
 KRONMULT_MODE_DETERMINISTIC = 1
+KRONMULT_NOALLOC_MAX_ENTRIES = 1048576
 
 
 class KronmultError(RuntimeError):
@@ -74,6 +75,7 @@ SIGNATURES = {
     "kronmult_tuning_cache_save": (_i, [ctypes.c_char_p]),
     "kronmult_tuning_cache_load": (_i, [ctypes.c_char_p]),
     "kronmult_device_error": (_i, [ctypes.POINTER(ctypes.c_int), _i]),
+    "kronmult_batched_f64_noalloc": (_i, [_i, _i, _vp, _i, _vp, _vp, _i, _vp]),
     "kronmult_diag_fp64_fma_gflops": (_i, [ctypes.POINTER(ctypes.c_double)]),
     "kronmult_pow_int": (ctypes.c_longlong, [_i, _i]),
     "kronmult_error_string": (ctypes.c_char_p, [_i]),
