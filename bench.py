@@ -13,6 +13,8 @@ value       GFLOP/s (algorithmic 2*d*n*N flops per entry) over K device-timed st
             flush is needed between steps)
 e2e         the same metric through the public API with host (pinned) buffers:
             each step copies the inputs and factors in and the outputs back
+            (api.forward_from_host: 8 pieces, copies overlapping the forward),
+            host wall clock per step including the final synchronisation
 roofline    the forward kernel against the roof that binds it; for FP64 that is the
             FP64 FMA pipe, measured live (HBM fraction reported beside it)
 cpu_baseline  the C oracle (a restatement of the reference's kronmult_omp) on the
@@ -55,6 +57,8 @@ def parse():
     p.add_argument("--dtype", choices=["f64", "f32"], default="f64")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--suite", action="store_true",
+                   help="measure every configuration, one JSON line each (diagnostic report)")
     p.add_argument("--scale", type=float, default=1.0,
                    help="shrink the number of outputs/entries (profiling runs only; not a bench value)")
     return p.parse_args()
@@ -201,11 +205,162 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def _timed(fn, stream, reps: int, warmup: int = 3) -> float:
+    """Mean milliseconds per call of fn (which enqueues on `stream`), CUDA events."""
+    import torch
+
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def suite(args):
+    """Every configuration, one JSON line each (diagnostic report, not the headline)."""
+    import ctypes
+
+    import torch
+
+    from kronmult_gb300 import DeviceBatch, _lib, adjoint, forward_f32_f64out
+    from kronmult_gb300 import grouped as G
+    from kronmult_gb300 import workloads as W
+    from oracle import oracle as O
+
+    lib = _lib.lib()
+    dev = torch.device("cuda", 0)
+    st = torch.cuda.Stream(dev)
+    g = ctypes.c_double(0)
+    lib.kronmult_diag_fp64_fma_gflops(ctypes.byref(g))
+    fp64_peak = g.value
+    try:
+        hbm_peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+    except (OSError, ValueError, KeyError):
+        hbm_peak = 6800.0
+    reps = max(3, args.steps)
+
+    def emit(name, b, ms, in_size, out_size, extra=None, launches=1):
+        fl = b.flops() if not isinstance(b, list) else sum(x.flops() for x in b)
+        by = (b.bytes(in_size, out_size) if not isinstance(b, list)
+              else sum(x.bytes(in_size, out_size) for x in b))
+        line = {"suite": name, "ms": ms, "gflops": fl / ms / 1e6, "gbytes_per_s": by / ms / 1e6,
+                "fp64_frac": fl / ms / 1e6 / fp64_peak, "hbm_frac": by / ms / 1e6 / hbm_peak,
+                "fp64_peak_gflops": fp64_peak, "hbm_peak_gbs": hbm_peak, "launches": launches}
+        line.update(extra or {})
+        print(json.dumps(line), flush=True)
+
+    # C1, C2: plain forward
+    for cname, fn in (("c1", W.config1), ("c2", W.config2)):
+        b = fn()
+        db = DeviceBatch.from_host(b, device=dev)
+        for pf in (0, 1):
+            tune = None if pf == 0 else {"prefetch": 1}
+            ms = _timed(lambda: db.forward(stream=st, tuning=tune), st, reps)
+            emit(f"{cname}_fwd_f64" + ("" if pf == 0 else "_single_slot"), b, ms, 8, 8)
+        if cname == "c2":
+            ms = _timed(lambda: lib.kronmult_batched_f64_noalloc(b.d, b.n, db.mat_ptrs.data_ptr(), b.stride,
+                                                                 db.in_ptrs.data_ptr(), db.out_ptrs.data_ptr(),
+                                                                 b.nb, st.cuda_stream), st, reps)
+            emit("c2_fwd_f64_noalloc", b, ms, 8, 8, launches=2)
+            db32 = DeviceBatch.from_host(b, device=dev, dtype=torch.float32)
+            ms = _timed(lambda: db32.forward(stream=st), st, reps)
+            db32.outputs.zero_()
+            db32.forward(stream=st)
+            db.outputs.zero_()
+            db.forward(stream=st)
+            torch.cuda.synchronize()
+            err = (torch.linalg.norm(db32.outputs.double() - db.outputs) / torch.linalg.norm(db.outputs)).item()
+            emit("c2_fwd_f32", b, ms, 4, 4, {"rel_l2_vs_fp64": err})
+            del db32
+        del db
+        torch.cuda.empty_cache()
+
+    # C3: grouped persistent launch, atomic and deterministic, replayed from a CUDA graph
+    groups = W.config3()
+    dbs = [DeviceBatch.from_host(x, device=dev) for x in groups]
+    ms_sep = _timed(lambda: [d.forward(stream=st) for d in dbs], st, reps)
+    emit("c3_separate_launches_f64", groups, ms_sep, 8, 8, launches=len(dbs))
+    for mode in ("atomic", "deterministic"):
+        plan = G.GroupedPlan(dbs, mode=mode)
+        with torch.cuda.stream(st):
+            plan.run(stream=st)
+        torch.cuda.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=st):
+            plan.run(stream=st)
+        ms = _timed(lambda: graph.replay(), torch.cuda.current_stream(), reps)
+        emit(f"c3_grouped_{mode}_graph_f64", groups, ms, 8, 8, {"plan": plan.info()})
+        plan.close()
+    del dbs
+    torch.cuda.empty_cache()
+
+    # C4: FP32 storage, FP32 / TF32 / BF16 contraction, FP64 outputs
+    b = W.config4()
+    ref = O.forward(b)
+    db = DeviceBatch.from_host(b, device=dev, dtype=torch.float32, out_dtype=torch.float64)
+    for cname, code in (("fp32", _lib.KRONMULT_COMPUTE_FP32), ("tf32", _lib.KRONMULT_COMPUTE_TF32),
+                        ("bf16", _lib.KRONMULT_COMPUTE_BF16)):
+        ms = _timed(lambda: forward_f32_f64out(db, compute=code, stream=st), st, reps)
+        db.outputs.zero_()
+        forward_f32_f64out(db, compute=code, stream=st)
+        torch.cuda.synchronize()
+        got = db.outputs.cpu().numpy()
+        emit(f"c4_fwd_{cname}", b, ms, 4, 8, {"rel_l2_vs_fp64": O.rel_l2(got, ref), "max_err_vs_fp64": O.max_rel(got, ref)})
+    del db
+    torch.cuda.empty_cache()
+
+    # C5: forward + adjoint; plain FP64 launches vs FP32 captured in one CUDA graph
+    b = W.config5()
+    gout = np.random.Generator(np.random.PCG64(1105)).standard_normal((b.n_out, b.N))
+    res = {}
+    for dt, captured in ((torch.float64, False), (torch.float32, True)):
+        db = DeviceBatch.from_host(b, device=dev, dtype=dt)
+        gt = torch.from_numpy(gout).to(dev, dt)
+        gin = torch.zeros_like(db.inputs)
+        gfa = torch.zeros_like(db.factors)
+
+        def step():
+            db.forward(stream=st)
+            adjoint(db, gt, gin, gfa, stream=st)
+
+        if captured:
+            with torch.cuda.stream(st):
+                step()
+            torch.cuda.synchronize()
+            graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(graph, stream=st):
+                step()
+            ms = _timed(lambda: graph.replay(), torch.cuda.current_stream(), reps)
+        else:
+            ms = _timed(step, st, reps)
+        db.outputs.zero_(); gin.zero_(); gfa.zero_()
+        with torch.cuda.stream(st):
+            step()
+        torch.cuda.synchronize()
+        res[dt] = (ms, db.outputs.double().cpu().numpy(), gin.double().cpu().numpy(), gfa.double().cpu().numpy())
+    (m64, y64, gi64, ga64), (m32, y32, gi32, ga32) = res[torch.float64], res[torch.float32]
+    emit("c5_fwd_adj_f64_plain", b, m64, 8, 8, {"adjoint_flops_note": "gflops counts forward flops only"},
+         launches=2)
+    emit("c5_fwd_adj_f32_graph", b, m32, 4, 4, {
+        "speedup_vs_plain_fp64": m64 / m32,
+        "rel_l2_vs_fp64": {"output": O.rel_l2(y32, y64), "grad_input": O.rel_l2(gi32, gi64),
+                           "grad_factors": O.rel_l2(ga32, ga64)}}, launches=2)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.suite:
+        suite(args)
         return
     import torch
 
@@ -263,25 +418,26 @@ def main():
     h2d = h_in.numel() * esize + h_fac.numel() * esize
     d2h = h_out.numel() * esize
 
-    def e2e_step():
-        db.inputs.copy_(h_in, non_blocking=True)
-        db.factors.copy_(h_fac, non_blocking=True)
-        db.forward(stream=stream)
-        h_out.copy_(db.outputs, non_blocking=True)
+    from kronmult_gb300.api import forward_from_host
 
-    with torch.cuda.stream(stream):
+    pipe_streams = (torch.cuda.Stream(dev), torch.cuda.Stream(dev), torch.cuda.Stream(dev))
+
+    def e2e_step():
+        # copies in, forward, copy out: pipelined in 8 pieces over three streams
+        forward_from_host(db, h_in, h_fac, h_out, chunks=8, streams=pipe_streams)
+
+    e2e_step()
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
         e2e_step()
-        torch.cuda.synchronize()
-        barrier()
-        t0 = time.perf_counter()
-        ee0 = torch.cuda.Event(enable_timing=True)
-        ee1 = torch.cuda.Event(enable_timing=True)
-        ee0.record(stream)
-        for _ in range(args.e2e_steps):
-            e2e_step()
-        ee1.record(stream)
-        stream.synchronize()
-    e2e_ms = max(ee0.elapsed_time(ee1), (time.perf_counter() - t0) * 1e3) / args.e2e_steps
+        torch.cuda.synchronize()  # the host result is complete at the end of every step
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.e2e_steps
+    if world > 1:
+        t = torch.tensor([e2e_ms], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = t.item()
     e2e_value = flops_step * world / (e2e_ms / 1e3) / 1e9
 
     # ---- live roofline denominators

@@ -156,6 +156,18 @@ def adjoint(b: DeviceBatch, grad_outputs: torch.Tensor, grad_inputs: torch.Tenso
     gout = grad_outputs.contiguous()
     if gout.dtype != dt or gout.shape[1] != N:
         raise ValueError("grad_outputs must be (n_out, N) of the batch dtype")
+    key = (gout.data_ptr(), None if grad_inputs is None else grad_inputs.data_ptr(),
+           None if grad_factors is None else grad_factors.data_ptr())
+    cached = getattr(b, "_adj_tables", None)
+    if cached is not None and cached[0] == key:
+        _, gout_ptrs, gin_ptrs, gmat_ptrs = cached
+        fn = getattr(_lib.lib(), name)
+        st = fn(b.d, b.n, b.mat_ptrs.data_ptr(), b.stride, b.in_ptrs.data_ptr(), gout_ptrs.data_ptr(),
+                None if gin_ptrs is None else gin_ptrs.data_ptr(),
+                None if gmat_ptrs is None else gmat_ptrs.data_ptr(), b.stride, b.nb, _stream_handle(stream),
+                _lib.tuning_ptr(tuning))
+        _lib.check(st, name)
+        return
     gout_ptrs = gout.data_ptr() + b.out_index * (N * es)
     gin_ptrs = None
     if grad_inputs is not None:
@@ -175,9 +187,10 @@ def adjoint(b: DeviceBatch, grad_outputs: torch.Tensor, grad_inputs: torch.Tenso
             None if gin_ptrs is None else gin_ptrs.data_ptr(), None if gmat_ptrs is None else gmat_ptrs.data_ptr(),
             b.stride, b.nb, _stream_handle(stream), _lib.tuning_ptr(tuning))
     _lib.check(st, name)
-    # the pointer tables are temporaries: keep them referenced (until the next call on this
-    # batch) so that the caching allocator cannot hand their memory out before the kernel reads it
-    b._keepalive = (gout, gout_ptrs, gin_ptrs, gmat_ptrs)
+    # keep the pointer tables referenced by the batch (reused while the same gradient
+    # tensors are passed) so that their memory stays valid for the enqueued kernel
+    b._adj_tables = (key, gout_ptrs, gin_ptrs, gmat_ptrs)
+    b._adj_keep = gout
 
 
 def forward_f32_f64out(b: DeviceBatch, compute: int = _lib.KRONMULT_COMPUTE_FP32, stream=None,
@@ -188,3 +201,63 @@ def forward_f32_f64out(b: DeviceBatch, compute: int = _lib.KRONMULT_COMPUTE_FP32
             None if b.ws_ptrs is None else b.ws_ptrs.data_ptr(), b.nb, int(compute), _stream_handle(stream),
             _lib.tuning_ptr(tuning))
     _lib.check(st, "kronmult_batched_f32_f64out_async")
+
+
+def forward_from_host(b: DeviceBatch, h_inputs: torch.Tensor, h_factors: torch.Tensor, h_outputs: torch.Tensor,
+                      chunks: int = 8, streams=None) -> None:
+    """End-to-end forward for a batch whose data lives in (pinned) host memory.
+
+    Copies factors and inputs into the batch's device tensors, runs the forward and
+    copies the outputs back into `h_outputs`, pipelined in `chunks` pieces cut at
+    output-group boundaries: the host-to-device copy of piece i+1 and the
+    device-to-host copy of piece i-1 overlap the forward of piece i.  When the
+    factor sets or the outputs are not used in increasing order, the factors are
+    copied before and the outputs after the whole batch instead.  Enqueues only;
+    synchronise with torch.cuda.synchronize()."""
+    dev = b.inputs.device
+    s_in, s_cmp, s_out = streams or (torch.cuda.Stream(dev), torch.cuda.Stream(dev), torch.cuda.Stream(dev))
+    nb = b.nb
+    out_idx = b.out_index
+    fac_idx = b.fac_index
+    # chunk boundaries at output-group starts (host copies of the small index maps)
+    oi = out_idx.cpu()
+    fi = fac_idx.cpu()
+    starts = torch.nonzero(torch.cat([torch.tensor([True]), oi[1:] != oi[:-1]])).flatten().tolist() + [nb]
+    ngroups = len(starts) - 1
+    chunks = max(1, min(chunks, ngroups))
+    cuts = [starts[(ngroups * c) // chunks] for c in range(chunks)] + [nb]
+    monotone = bool(torch.all(fi[1:] >= fi[:-1])) if nb > 1 else True
+    out_monotone = bool(torch.all(oi[1:] >= oi[:-1])) if nb > 1 else True
+    d = b.d
+    if not monotone:
+        with torch.cuda.stream(s_in):
+            b.factors.copy_(h_factors, non_blocking=True)
+    ev_in = [torch.cuda.Event() for _ in range(chunks)]
+    ev_cmp = [torch.cuda.Event() for _ in range(chunks)]
+    for c in range(chunks):
+        lo, hi = cuts[c], cuts[c + 1]
+        if hi <= lo:
+            continue
+        with torch.cuda.stream(s_in):
+            b.inputs[lo:hi].copy_(h_inputs[lo:hi], non_blocking=True)
+            if monotone:
+                f0, f1 = int(fi[lo]) * d, (int(fi[hi - 1]) + 1) * d
+                b.factors[f0:f1].copy_(h_factors[f0:f1], non_blocking=True)
+            ev_in[c].record(s_in)
+        s_cmp.wait_event(ev_in[c])
+        es_p = b.mat_ptrs.element_size()
+        fn = getattr(_lib.lib(), _FN[b.inputs.dtype] + "_async")
+        st = fn(b.d, b.n, b.mat_ptrs.data_ptr() + lo * d * es_p, b.stride, b.in_ptrs.data_ptr() + lo * es_p,
+                b.out_ptrs.data_ptr() + lo * es_p, None, hi - lo, s_cmp.cuda_stream, None)
+        _lib.check(st, "kronmult_batched_async")
+        ev_cmp[c].record(s_cmp)
+        if out_monotone:
+            s_out.wait_event(ev_cmp[c])
+            o0, o1 = int(oi[lo]), int(oi[hi - 1]) + 1
+            with torch.cuda.stream(s_out):
+                h_outputs[o0:o1].copy_(b.outputs[o0:o1], non_blocking=True)
+    if not out_monotone:
+        s_out.wait_stream(s_cmp)
+        with torch.cuda.stream(s_out):
+            h_outputs.copy_(b.outputs, non_blocking=True)
+    return s_in, s_cmp, s_out
