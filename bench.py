@@ -59,6 +59,8 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=5)
     p.add_argument("--suite", action="store_true",
                    help="measure every configuration, one JSON line each (diagnostic report)")
+    p.add_argument("--only", default="",
+                   help="with --suite: run only the items whose name starts with this prefix (c1, c2, c3, c4, c5)")
     p.add_argument("--scale", type=float, default=1.0,
                    help="shrink the number of outputs/entries (profiling runs only; not a bench value)")
     return p.parse_args()
@@ -244,6 +246,10 @@ def suite(args):
     except (OSError, ValueError, KeyError):
         hbm_peak = 6800.0
     reps = max(3, args.steps)
+    sc = args.scale
+
+    def want(prefix):
+        return not args.only or prefix.startswith(args.only) or args.only.startswith(prefix)
 
     def emit(name, b, ms, in_size, out_size, extra=None, launches=1):
         fl = b.flops() if not isinstance(b, list) else sum(x.flops() for x in b)
@@ -257,7 +263,9 @@ def suite(args):
 
     # C1, C2: plain forward
     for cname, fn in (("c1", W.config1), ("c2", W.config2)):
-        b = fn()
+        if not want(cname):
+            continue
+        b = fn(scale=sc)
         db = DeviceBatch.from_host(b, device=dev)
         for pf in (0, 1):
             tune = None if pf == 0 else {"prefetch": 1}
@@ -282,11 +290,12 @@ def suite(args):
         torch.cuda.empty_cache()
 
     # C3: grouped persistent launch, atomic and deterministic, replayed from a CUDA graph
-    groups = W.config3()
+    groups = W.config3(scale=sc) if want("c3") else []
     dbs = [DeviceBatch.from_host(x, device=dev) for x in groups]
-    ms_sep = _timed(lambda: [d.forward(stream=st) for d in dbs], st, reps)
-    emit("c3_separate_launches_f64", groups, ms_sep, 8, 8, launches=len(dbs))
-    for mode in ("atomic", "deterministic"):
+    if groups:
+        ms_sep = _timed(lambda: [d.forward(stream=st) for d in dbs], st, reps)
+        emit("c3_separate_launches_f64", groups, ms_sep, 8, 8, launches=len(dbs))
+    for mode in ("atomic", "deterministic") if groups else ():
         plan = G.GroupedPlan(dbs, mode=mode)
         with torch.cuda.stream(st):
             plan.run(stream=st)
@@ -301,11 +310,12 @@ def suite(args):
     torch.cuda.empty_cache()
 
     # C4: FP32 storage, FP32 / TF32 / BF16 contraction, FP64 outputs
-    b = W.config4()
-    ref = O.forward(b)
-    db = DeviceBatch.from_host(b, device=dev, dtype=torch.float32, out_dtype=torch.float64)
-    for cname, code in (("fp32", _lib.KRONMULT_COMPUTE_FP32), ("tf32", _lib.KRONMULT_COMPUTE_TF32),
-                        ("bf16", _lib.KRONMULT_COMPUTE_BF16)):
+    modes4 = [(c, k) for c, k in (("fp32", _lib.KRONMULT_COMPUTE_FP32), ("tf32", _lib.KRONMULT_COMPUTE_TF32),
+                                  ("bf16", _lib.KRONMULT_COMPUTE_BF16)) if want(f"c4_fwd_{c}")]
+    b = W.config4(scale=sc) if modes4 else None
+    ref = O.forward(b) if modes4 else None
+    db = DeviceBatch.from_host(b, device=dev, dtype=torch.float32, out_dtype=torch.float64) if modes4 else None
+    for cname, code in modes4:
         ms = _timed(lambda: forward_f32_f64out(db, compute=code, stream=st), st, reps)
         db.outputs.zero_()
         forward_f32_f64out(db, compute=code, stream=st)
@@ -316,7 +326,9 @@ def suite(args):
     torch.cuda.empty_cache()
 
     # C5: forward + adjoint; plain FP64 launches vs FP32 captured in one CUDA graph
-    b = W.config5()
+    if not want("c5"):
+        return
+    b = W.config5(scale=sc)
     gout = np.random.Generator(np.random.PCG64(1105)).standard_normal((b.n_out, b.N))
     res = {}
     for dt, captured in ((torch.float64, False), (torch.float32, True)):
