@@ -161,7 +161,9 @@ __device__ __forceinline__ void team_forward(const T *const *mats, const T *cons
     // PF: two staging slots (buf/fac and buf2/fac2); the copies of entry e+1 are in
     // flight (cp.async) while entry e is computed
     const int F = N / NN;
-    TO acc[QMAX][NN];
+    // a run of entries is summed in the compute type (FP32 accumulation for FP32
+    // storage); the output type is used only for the final addition into the output
+    T acc[QMAX][NN];
     TO *cur = nullptr;
 
     auto flush = [&](TO *dst) {
@@ -172,9 +174,9 @@ __device__ __forceinline__ void team_forward(const T *const *mats, const T *cons
 #pragma unroll
                 for (int r = 0; r < NN; ++r) {
                     if constexpr (DET) {
-                        dst[c + r * F] = dst[c + r * F] + acc[q][r];
+                        dst[c + r * F] = dst[c + r * F] + (TO)acc[q][r];
                     } else {
-                        atomic_add<TO>(dst + c + r * F, acc[q][r]);
+                        atomic_add<TO>(dst + c + r * F, (TO)acc[q][r]);
                     }
                 }
             }
@@ -252,12 +254,12 @@ __device__ __forceinline__ void team_forward(const T *const *mats, const T *cons
 #pragma unroll
             for (int q = 0; q < QMAX; ++q)
 #pragma unroll
-                for (int r = 0; r < NN; ++r) acc[q][r] = (TO)y[q][r];
+                for (int r = 0; r < NN; ++r) acc[q][r] = y[q][r];
         } else {
 #pragma unroll
             for (int q = 0; q < QMAX; ++q)
 #pragma unroll
-                for (int r = 0; r < NN; ++r) acc[q][r] += (TO)y[q][r];
+                for (int r = 0; r < NN; ++r) acc[q][r] += y[q][r];
         }
         if constexpr (PF) {
             T *t = buf;
@@ -271,8 +273,9 @@ __device__ __forceinline__ void team_forward(const T *const *mats, const T *cons
     if (cur != nullptr) flush(cur);
 }
 
+// FP32 variants are capped at 64 registers so that four 256-thread CTAs fit on an SM
 template <typename T, typename TO, int NN, int QMAX>
-__global__ void __launch_bounds__(512) fwd_smem_kernel(const FwdArgs<T, TO> a)
+__global__ void __launch_bounds__(512, sizeof(T) == 4 ? 2 : 1) fwd_smem_kernel(const FwdArgs<T, TO> a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const Team tm(a.team_size);

@@ -15,7 +15,7 @@
 //
 // One CTA = one warpgroup (128 threads) works on one entry at a time; several
 // CTAs per SM overlap the input loads.  Consecutive entries with the same
-// output pointer are summed in FP64 registers and added with FP64 atomics.
+// output pointer are summed in FP32 registers and added with FP64 atomics.
 //
 // Every wait on an mbarrier is bounded; on timeout the kernel records an error
 // code in a device word (kronmult_device_error) and leaves after freeing its
@@ -184,7 +184,7 @@ template <int KIND> __global__ void __launch_bounds__(kTcThreads) fwd_tc_kernel(
     bool failed = false;
 
     constexpr int MAXT = 4;  // tiles per entry held in registers (N <= 4096)
-    double acc[MAXT][8];
+    float acc[MAXT][8];  // a run of entries is summed in FP32; FP64 only in the output atomics
     double *cur = nullptr;
 
     for (; e < e_end && !failed; ++e) {
@@ -262,19 +262,19 @@ template <int KIND> __global__ void __launch_bounds__(kTcThreads) fwd_tc_kernel(
                     const int c = t * kTileRows + warp * 32 + lane;
                     if (t < a.tiles && c < F)
 #pragma unroll
-                        for (int r = 0; r < 8; ++r) atomicAdd(cur + c + r * F, acc[t][r]);
+                        for (int r = 0; r < 8; ++r) atomicAdd(cur + c + r * F, (double)acc[t][r]);
                 }
             }
             cur = o;
 #pragma unroll
             for (int t = 0; t < MAXT; ++t)
 #pragma unroll
-                for (int r = 0; r < 8; ++r) acc[t][r] = (double)v[t][r];
+                for (int r = 0; r < 8; ++r) acc[t][r] = v[t][r];
         } else {
 #pragma unroll
             for (int t = 0; t < MAXT; ++t)
 #pragma unroll
-                for (int r = 0; r < 8; ++r) acc[t][r] += (double)v[t][r];
+                for (int r = 0; r < 8; ++r) acc[t][r] += v[t][r];
         }
     }
     if (cur != nullptr && !failed) {
@@ -283,7 +283,7 @@ template <int KIND> __global__ void __launch_bounds__(kTcThreads) fwd_tc_kernel(
             const int c = t * kTileRows + warp * 32 + lane;
             if (t < a.tiles && c < F)
 #pragma unroll
-                for (int r = 0; r < 8; ++r) atomicAdd(cur + c + r * F, acc[t][r]);
+                for (int r = 0; r < 8; ++r) atomicAdd(cur + c + r * F, (double)acc[t][r]);
         }
     }
     tc_fence_before();
