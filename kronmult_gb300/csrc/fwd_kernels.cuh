@@ -295,6 +295,65 @@ __global__ void __launch_bounds__(512, sizeof(T) == 4 ? 2 : 1) fwd_smem_kernel(c
     }
 }
 
+// One entry per team, no run accumulator and no second staging slot: fewer
+// registers and less shared memory, so more CTAs per SM.  The hardware block
+// scheduler then overlaps one CTA's staging with other CTAs' compute.  Teams of
+// at most 256 threads.
+template <typename T, typename TO, int NN, int QMAX>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) fwd_single_kernel(const FwdArgs<T, TO> a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const Team tm(a.team_size);
+    T *buf = reinterpret_cast<T *>(smem_raw) + (size_t)tm.id * a.team_elems;
+    T *fac = buf + a.vec_pad;
+    const long long e = (long long)blockIdx.x * a.teams_per_cta + tm.id;
+    if (e >= a.nb) return;
+    const int F = a.N / NN;
+    stage_vector(buf, a.in[e], a.N, tm);
+    stage_factors<T, NN>(fac, a.mats + e * a.d, a.d, a.stride, tm);
+    tm.sync();
+    T y[QMAX][NN];
+    for (int i = a.d - 1; i >= 0; --i) {
+        const T *M = fac + i * NN * NN;
+#pragma unroll
+        for (int q = 0; q < QMAX; ++q) {
+            const int c = tm.rank + q * tm.size;
+            if (c < F) {
+                T xv[NN];
+                load_fibre<T, NN>(buf + c * NN, xv);
+#pragma unroll
+                for (int r = 0; r < NN; ++r) {
+                    T s = T(0);
+#pragma unroll
+                    for (int k = 0; k < NN; ++k) s = fma_t<T>(M[r + k * NN], xv[k], s);
+                    y[q][r] = s;
+                }
+            }
+        }
+        if (i > 0) {
+            tm.sync();
+#pragma unroll
+            for (int q = 0; q < QMAX; ++q) {
+                const int c = tm.rank + q * tm.size;
+                if (c < F) {
+#pragma unroll
+                    for (int r = 0; r < NN; ++r) buf[c + r * F] = y[q][r];
+                }
+            }
+            tm.sync();
+        }
+    }
+    TO *o = a.out[e];
+#pragma unroll
+    for (int q = 0; q < QMAX; ++q) {
+        const int c = tm.rank + q * tm.size;
+        if (c < F) {
+#pragma unroll
+            for (int r = 0; r < NN; ++r) atomic_add<TO>(o + c + r * F, (TO)y[q][r]);
+        }
+    }
+}
+
 // ---- generic kernel (runtime n, any N) ------------------------------------
 //
 // One CTA per entry (grid-stride over entries), one thread per output element.
@@ -349,6 +408,7 @@ __global__ void __launch_bounds__(256) fwd_generic_kernel(const FwdArgs<T, TO> a
 // kernel pointer lookup, defined once per (T, TO) instantiation unit
 template <typename T, typename TO> using FwdSmemFn = void (*)(const FwdArgs<T, TO>);
 template <typename T, typename TO> FwdSmemFn<T, TO> fwd_smem_lookup(int nn, int qmax);
+template <typename T, typename TO> FwdSmemFn<T, TO> fwd_single_lookup(int nn, int qmax);
 template <typename T, typename TO> void *fwd_generic_ptr();
 
 }  // namespace kgb
@@ -383,6 +443,36 @@ template <typename T, typename TO> void *fwd_generic_ptr();
         case 8 * 16 + 1: return fwd_smem_kernel<T, TO, 8, 1>;                                          \
         case 8 * 16 + 2: return fwd_smem_kernel<T, TO, 8, 2>;                                          \
         case 8 * 16 + 4: return fwd_smem_kernel<T, TO, 8, 4>;                                          \
+        default: return nullptr;                                                                       \
+        }                                                                                              \
+    }                                                                                                  \
+    template <> FwdSmemFn<T, TO> fwd_single_lookup<T, TO>(int nn, int qmax)                           \
+    {                                                                                                  \
+        switch (nn * 16 + qmax) {                                                                      \
+        case 2 * 16 + 1: return fwd_single_kernel<T, TO, 2, 1>;                                        \
+        case 2 * 16 + 2: return fwd_single_kernel<T, TO, 2, 2>;                                        \
+        case 2 * 16 + 4: return fwd_single_kernel<T, TO, 2, 4>;                                        \
+        case 2 * 16 + 8: return fwd_single_kernel<T, TO, 2, 8>;                                        \
+        case 3 * 16 + 1: return fwd_single_kernel<T, TO, 3, 1>;                                        \
+        case 3 * 16 + 2: return fwd_single_kernel<T, TO, 3, 2>;                                        \
+        case 3 * 16 + 4: return fwd_single_kernel<T, TO, 3, 4>;                                        \
+        case 3 * 16 + 8: return fwd_single_kernel<T, TO, 3, 8>;                                        \
+        case 4 * 16 + 1: return fwd_single_kernel<T, TO, 4, 1>;                                        \
+        case 4 * 16 + 2: return fwd_single_kernel<T, TO, 4, 2>;                                        \
+        case 4 * 16 + 4: return fwd_single_kernel<T, TO, 4, 4>;                                        \
+        case 4 * 16 + 8: return fwd_single_kernel<T, TO, 4, 8>;                                        \
+        case 5 * 16 + 1: return fwd_single_kernel<T, TO, 5, 1>;                                        \
+        case 5 * 16 + 2: return fwd_single_kernel<T, TO, 5, 2>;                                        \
+        case 5 * 16 + 4: return fwd_single_kernel<T, TO, 5, 4>;                                        \
+        case 6 * 16 + 1: return fwd_single_kernel<T, TO, 6, 1>;                                        \
+        case 6 * 16 + 2: return fwd_single_kernel<T, TO, 6, 2>;                                        \
+        case 6 * 16 + 4: return fwd_single_kernel<T, TO, 6, 4>;                                        \
+        case 7 * 16 + 1: return fwd_single_kernel<T, TO, 7, 1>;                                        \
+        case 7 * 16 + 2: return fwd_single_kernel<T, TO, 7, 2>;                                        \
+        case 7 * 16 + 4: return fwd_single_kernel<T, TO, 7, 4>;                                        \
+        case 8 * 16 + 1: return fwd_single_kernel<T, TO, 8, 1>;                                        \
+        case 8 * 16 + 2: return fwd_single_kernel<T, TO, 8, 2>;                                        \
+        case 8 * 16 + 4: return fwd_single_kernel<T, TO, 8, 4>;                                        \
         default: return nullptr;                                                                       \
         }                                                                                              \
     }                                                                                                  \

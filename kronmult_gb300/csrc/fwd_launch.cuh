@@ -102,10 +102,48 @@ int plan_forward(FwdPlan<T, TO> &pl, int d, int n, const T *const *mats, int str
             const int qtarget = (n <= 4) ? 4 : 2;
             while (ts < 512 && (long long)ts * qtarget < F) ts *= 2;
         }
+        // One entry per team (fwd_single_kernel) unless runs are requested: measured
+        // fastest for FP64, where the FP64 pipe is the bound and more resident CTAs
+        // hide the staging; FP32 sums runs of 8 entries by default.
+        bool single = tune && tune->entries_per_team > 0 ? tune->entries_per_team == 1 : sizeof(T) == 8;
+        const int ts_runs = ts;
+        if (single && ts > 256) {
+            ts = 256;  // the single-entry kernel runs teams of at most 256 threads
+            if ((F + ts - 1) / ts > qcap) {
+                single = false;
+                ts = ts_runs;
+            }
+        }
         const int q = (F + ts - 1) / ts;
         int qmax = 1;
         while (qmax < q) qmax *= 2;
         const bool ts_ok = (ts == 8 || ts == 16 || ts == 32 || ts == 64 || ts == 128 || ts == 256 || ts == 512);
+        if (single && ts_ok && qmax <= qcap) {
+            const int vpad = round_up(N, 16 / (int)sizeof(T));
+            const int fpad = round_up(d * n * n, 16 / (int)sizeof(T));
+            const int team_elems = vpad + fpad;
+            const int teams = 256 / ts;
+            const size_t smem = (size_t)teams * team_elems * sizeof(T);
+            auto fn = fwd_single_lookup<T, TO>(n, qmax);
+            if (fn && smem <= (size_t)di.max_smem_optin && ensure_smem_attr((const void *)fn, smem)) {
+                const long long grid = (nb + teams - 1) / teams;
+                if (grid <= INT_MAX) {
+                    a.team_size = ts;
+                    a.teams_per_cta = teams;
+                    a.entries_per_team = 1;
+                    a.team_elems = team_elems;
+                    a.vec_pad = vpad;
+                    a.fac_pad = fpad;
+                    a.prefetch = 0;
+                    pl.fn = (const void *)fn;
+                    pl.smem_path = true;
+                    pl.grid = dim3((unsigned)grid);
+                    pl.block = dim3((unsigned)(teams * ts));
+                    pl.smem = smem;
+                    return cudaSuccess;
+                }
+            }
+        }
         if (ts_ok && qmax <= qcap) {
             const int vpad = round_up(N, 16 / (int)sizeof(T));
             const int fpad = round_up(d * n * n, 16 / (int)sizeof(T));
@@ -135,8 +173,8 @@ int plan_forward(FwdPlan<T, TO> &pl, int d, int n, const T *const *mats, int str
                                                                  : occupancy((const void *)fn, block, smem);
                     if (per_sm < 1) per_sm = 1;
                     const long long total_teams = (long long)di.sms * per_sm * teams;
-                    long long ept = (tune && tune->entries_per_team > 0) ? tune->entries_per_team
-                                                                         : (nb + total_teams - 1) / total_teams;
+                    long long ept = (tune && tune->entries_per_team > 0) ? tune->entries_per_team : 8;
+                    if (ept * total_teams > nb * 2) ept = (nb + total_teams - 1) / total_teams;  // small batches
                     if (ept < 1) ept = 1;
                     if (ept > INT_MAX) ept = INT_MAX;
                     const long long per_cta = ept * teams;

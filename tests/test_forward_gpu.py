@@ -98,6 +98,21 @@ def test_team_sizes_agree(cuda, team_size, prefetch):
     assert O.rel_l2(got, O.forward(b)) <= TOL64
 
 
+@pytest.mark.parametrize("ept", [1, 2, 8])
+@pytest.mark.parametrize("team_size", [8, 32, 128, 256])
+def test_single_entry_and_run_kernels(cuda, team_size, ept):
+    """entries_per_team = 1 selects the single-entry kernel, larger values the
+    run-accumulating one; both dtypes, all agree with the oracle."""
+    from kronmult_gb300 import workloads as W
+
+    b = W.make_batch(4, 4, 6, 9, 5, seed=300 + team_size)
+    t = {"team_size": team_size, "entries_per_team": ept}
+    got, _ = run(b, cuda, tuning=t)
+    assert O.rel_l2(got, O.forward(b)) <= TOL64
+    got32, _ = run(b, cuda, dtype=torch.float32, tuning=t)
+    assert O.rel_l2(got32, O.forward(b)) <= TOL32
+
+
 @pytest.mark.parametrize("n", [2, 3, 5, 6, 7, 8])
 def test_prefetch_odd_sizes(cuda, n):
     """Unaligned vector lengths take the element-wise asynchronous copy."""
