@@ -4,6 +4,7 @@
 #include <cstdint>
 #include <mutex>
 #include "fwd_kernels.cuh"
+#include "pair_kernels.cuh"
 #include "kronmult_gb300.h"
 #include "tuning.cuh"
 
@@ -141,6 +142,48 @@ int plan_forward(FwdPlan<T, TO> &pl, int d, int n, const T *const *mats, int str
                     pl.block = dim3((unsigned)(teams * ts));
                     pl.smem = smem;
                     return cudaSuccess;
+                }
+            }
+        }
+        // FP32, n = 2 or 4, d >= 2: two modes per shared-memory pass (fwd_pair_kernel)
+        if constexpr (sizeof(T) == 4) {
+            const bool want_pair = !single && (n == 2 || n == 4) && d >= 2 && !(tune && tune->prefetch == 1) &&
+                                   !(tune && tune->team_size > 0);
+            if (want_pair) {
+                const int F2 = N / (n * n);
+                int tsp = 8;
+                while (tsp < 256 && tsp * 2 < F2) tsp *= 2;
+                const int qp = (F2 + tsp - 1) / tsp;
+                auto fn = qp <= 2 ? fwd_pair_lookup<TO>(n, qp <= 1 ? 1 : 2) : nullptr;
+                const int vpad = round_up(N, 4);
+                const int fpad = round_up(d * n * n, 4);
+                const int team_elems = 2 * (vpad + fpad);
+                const int teams = 256 / tsp;
+                const size_t smem = (size_t)teams * team_elems * sizeof(T);
+                if (fn && smem <= (size_t)di.max_smem_optin && ensure_smem_attr((const void *)fn, smem)) {
+                    int per_sm = (tune && tune->ctas_per_sm > 0) ? tune->ctas_per_sm
+                                                                 : occupancy((const void *)fn, teams * tsp, smem);
+                    if (per_sm < 1) per_sm = 1;
+                    const long long total_teams = (long long)di.sms * per_sm * teams;
+                    long long ept = (tune && tune->entries_per_team > 0) ? tune->entries_per_team : 8;
+                    if (ept * total_teams > nb * 2) ept = (nb + total_teams - 1) / total_teams;
+                    if (ept < 1) ept = 1;
+                    const long long grid = (nb + ept * teams - 1) / (ept * teams);
+                    if (grid <= INT_MAX && ept <= INT_MAX) {
+                        a.team_size = tsp;
+                        a.teams_per_cta = teams;
+                        a.entries_per_team = (int)ept;
+                        a.team_elems = team_elems;
+                        a.vec_pad = vpad;
+                        a.fac_pad = fpad;
+                        a.prefetch = 1;
+                        pl.fn = (const void *)fn;
+                        pl.smem_path = true;
+                        pl.grid = dim3((unsigned)grid);
+                        pl.block = dim3((unsigned)(teams * tsp));
+                        pl.smem = smem;
+                        return cudaSuccess;
+                    }
                 }
             }
         }

@@ -221,3 +221,18 @@ def test_cpp_drop_in_runs(cuda, tmp_path):
     exe = build_drop_in(tmp_path)
     p = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     assert p.returncode == 0, p.stdout + p.stderr
+
+
+@pytest.mark.parametrize("n,d", [(2, 2), (2, 3), (2, 9), (4, 2), (4, 3), (4, 5), (4, 6)])
+def test_fp32_two_modes_per_pass(cuda, n, d):
+    """FP32 n = 2, 4 runs two modes per shared-memory pass (odd d: one single step
+    first); same result as the oracle's FP32 sweep up to FP32 rounding."""
+    from kronmult_gb300 import workloads as W
+
+    b = W.make_batch(d, n, n + 3, 6, 7, seed=400 + 10 * n + d)
+    ref32 = O.forward(b, dtype=np.float32)
+    got, _ = run(b, cuda, dtype=torch.float32)
+    assert O.rel_l2(got, ref32) <= 1e-6
+    assert O.rel_l2(got, O.forward(b)) <= TOL32
+    got64o, _ = run(b, cuda, dtype=torch.float32, out_dtype=torch.float64)
+    assert O.rel_l2(got64o, O.forward(b)) <= TOL32
