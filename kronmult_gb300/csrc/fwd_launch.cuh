@@ -152,7 +152,7 @@ int plan_forward(FwdPlan<T, TO> &pl, int d, int n, const T *const *mats, int str
             if (want_pair) {
                 const int F2 = N / (n * n);
                 int tsp = 8;
-                while (tsp < 256 && tsp * 2 < F2) tsp *= 2;
+                while (tsp < 256 && tsp < F2) tsp *= 2;  // one bi-fibre per thread up to 256 threads
                 const int qp = (F2 + tsp - 1) / tsp;
                 auto fn = qp <= 2 ? fwd_pair_lookup<TO>(n, qp <= 1 ? 1 : 2) : nullptr;
                 const int vpad = round_up(N, 4);

@@ -39,21 +39,53 @@ template <int NN> struct PairSwizzle {
     }
 };
 
+// Pointers of one entry as seen by one thread: its input vector and the factor
+// matrices of the (at most kPairFacSlots) factor elements this thread copies.
+// They are loaded one entry ahead of the copy that uses them, so that the copy is
+// not stalled behind dependent pointer-table loads.
+constexpr int kPairFacSlots = 1;
+struct PairPtrs {
+    const float *src;
+    const float *mat[kPairFacSlots];
+};
+
+template <int NN>
+__device__ __forceinline__ void pair_load_ptrs(PairPtrs &p, const float *const *in, const float *const *mats,
+                                               long long e, int d, const Team &tm)
+{
+    constexpr int NN2 = NN * NN;
+    p.src = in[e];
+#pragma unroll
+    for (int s = 0; s < kPairFacSlots; ++s) {
+        const int idx = tm.rank + s * tm.size;
+        p.mat[s] = idx < d * NN2 ? mats[e * d + idx / NN2] : nullptr;
+    }
+}
+
 // stage one entry (vector in the swizzled layout, factors plain) asynchronously
 template <int NN>
-__device__ __forceinline__ void pair_stage_async(float *dst, float *fac, const float *src, const float *const *mats,
-                                                 int N, int d, int stride, const Team &tm)
+__device__ __forceinline__ void pair_stage_async(float *dst, float *fac, const PairPtrs &p,
+                                                 const float *const *mats_e, int N, int d, int stride, const Team &tm)
 {
-    if (((reinterpret_cast<uintptr_t>(src) & 15u) == 0) && ((N & 3) == 0)) {
+    if (((reinterpret_cast<uintptr_t>(p.src) & 15u) == 0) && ((N & 3) == 0)) {
         for (int v = tm.rank; v < N / 4; v += tm.size)
-            cp_async<16>(dst + 4 * PairSwizzle<NN>::chunk(v), src + 4 * v);
+            cp_async<16>(dst + 4 * PairSwizzle<NN>::chunk(v), p.src + 4 * v);
     } else {
-        for (int v = tm.rank; v < N; v += tm.size) cp_async<4>(dst + PairSwizzle<NN>::elem(v), src + v);
+        for (int v = tm.rank; v < N; v += tm.size) cp_async<4>(dst + PairSwizzle<NN>::elem(v), p.src + v);
     }
     constexpr int NN2 = NN * NN;
-    for (int idx = tm.rank; idx < d * NN2; idx += tm.size) {
+#pragma unroll
+    for (int s = 0; s < kPairFacSlots; ++s) {
+        const int idx = tm.rank + s * tm.size;
+        if (idx < d * NN2) {
+            const int rem = idx % NN2, k = rem / NN, r = rem - k * NN;
+            cp_async<4>(fac + idx, p.mat[s] + r + (size_t)k * stride);
+        }
+    }
+    // elements beyond the prefetched slots (small teams only): direct pointer loads
+    for (int idx = tm.rank + kPairFacSlots * tm.size; idx < d * NN2; idx += tm.size) {
         const int i = idx / NN2, rem = idx - i * NN2, k = rem / NN, r = rem - k * NN;
-        cp_async<4>(fac + idx, mats[i] + r + (size_t)k * stride);
+        cp_async<4>(fac + idx, mats_e[i] + r + (size_t)k * stride);
     }
     cp_async_commit();
 }
@@ -73,12 +105,21 @@ __device__ __forceinline__ void team_forward_pairs(const float *const *mats, con
     float acc[QP][NN2];
     TO *cur = nullptr;
 
-    if (e_begin < e_end) pair_stage_async<NN>(buf, fac, in[e_begin], mats + e_begin * d, N, d, stride, tm);
+    PairPtrs nxt;
+    if (e_begin < e_end) {
+        pair_load_ptrs<NN>(nxt, in, mats, e_begin, d, tm);
+        pair_stage_async<NN>(buf, fac, nxt, mats + e_begin * d, N, d, stride, tm);
+        if (e_begin + 1 < e_end) pair_load_ptrs<NN>(nxt, in, mats, e_begin + 1, d, tm);
+    }
     for (long long e = e_begin; e < e_end; ++e) {
         TO *o = out[e];
         cp_async_wait_all();
         tm.sync();
-        if (e + 1 < e_end) pair_stage_async<NN>(buf2, fac2, in[e + 1], mats + (e + 1) * d, N, d, stride, tm);
+        if (e + 1 < e_end) {
+            pair_stage_async<NN>(buf2, fac2, nxt, mats + (e + 1) * d, N, d, stride, tm);
+            // pointers of entry e+2: in flight while entry e is computed
+            if (e + 2 < e_end) pair_load_ptrs<NN>(nxt, in, mats, e + 2, d, tm);
+        }
 
         int i = d - 1;
         if (d & 1) {
