@@ -152,12 +152,15 @@ __device__ __forceinline__ void team_forward_pairs(const float *const *mats, con
                 }
             }
             tm.sync();
+            // when F is a multiple of 256 the swizzle of c + r*F is the swizzle of c plus r*F
+            const bool linear1 = NN != 4 || (F & 255) == 0;
 #pragma unroll
             for (int q = 0; q < Q1; ++q) {
                 const int c = tm.rank + q * tm.size;
                 if (c < F) {
+                    const int base = SW::elem(c);
 #pragma unroll
-                    for (int r = 0; r < NN; ++r) buf[SW::elem(c + r * F)] = y[q][r];
+                    for (int r = 0; r < NN; ++r) buf[linear1 ? base + r * F : SW::elem(c + r * F)] = y[q][r];
                 }
             }
             tm.sync();
@@ -217,12 +220,15 @@ __device__ __forceinline__ void team_forward_pairs(const float *const *mats, con
             }
             tm.sync();  // every read of buf (and fac) for this pass is done
             if (i > 1) {
+                // when F2 is a multiple of 256 the swizzle of c2 + j*F2 is the swizzle of c2 plus j*F2
+                const bool linear2 = NN != 4 || (F2 & 255) == 0;
 #pragma unroll
                 for (int q = 0; q < QP; ++q) {
                     const int c2 = tm.rank + q * tm.size;
                     if (c2 < F2) {
+                        const int base = SW::elem(c2);
 #pragma unroll
-                        for (int j = 0; j < NN2; ++j) buf[SW::elem(c2 + F2 * j)] = z[q][j];
+                        for (int j = 0; j < NN2; ++j) buf[linear2 ? base + F2 * j : SW::elem(c2 + F2 * j)] = z[q][j];
                     }
                 }
                 tm.sync();
