@@ -147,23 +147,66 @@ struct TcArgs {
     int d, stride, N, tiles, tmem_cols, entries_per_cta;
 };
 
-template <int KIND> __global__ void __launch_bounds__(kTcThreads) fwd_tc_kernel(const TcArgs a)
+// per-thread pointers of one entry, loaded one entry ahead of the copies that use them
+constexpr int kTcFacSlots = 2;  // factor elements per thread: d*64 <= 256 = 2 x 128 threads
+struct TcPtrs {
+    const float *src;
+    const float *mat[kTcFacSlots];
+};
+
+__device__ __forceinline__ void tc_load_ptrs(TcPtrs &p, const TcArgs &a, long long e, int tid)
+{
+    p.src = a.in[e];
+#pragma unroll
+    for (int s = 0; s < kTcFacSlots; ++s) {
+        const int idx = tid + s * kTcThreads;
+        p.mat[s] = idx < a.d * 64 ? a.mats[e * a.d + (idx >> 6)] : nullptr;
+    }
+}
+
+// asynchronous copy of one entry into a raw staging slot: the vector in natural
+// order, the factors as fraw[i*64 + r + 8k] = A_i(r, k)
+__device__ __forceinline__ void tc_stage_async(float *raw, float *fraw, const TcPtrs &p, const TcArgs &a, int tid)
+{
+    const int N = a.N;
+    if (((reinterpret_cast<uintptr_t>(p.src) & 15u) == 0) && ((N & 3) == 0)) {
+        for (int q = tid; q < N / 4; q += kTcThreads) cp_async<16>(raw + 4 * q, p.src + 4 * q);
+    } else {
+        for (int q = tid; q < N; q += kTcThreads) cp_async<4>(raw + q, p.src + q);
+    }
+#pragma unroll
+    for (int s = 0; s < kTcFacSlots; ++s) {
+        const int idx = tid + s * kTcThreads;
+        if (idx < a.d * 64) {
+            const int r = idx & 7, k = (idx >> 3) & 7;
+            cp_async<4>(fraw + idx, p.mat[s] + r + (size_t)k * a.stride);
+        }
+    }
+    cp_async_commit();
+}
+
+template <int KIND> __global__ void __launch_bounds__(kTcThreads, 4) fwd_tc_kernel(const TcArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    unsigned char *xs = smem_raw;                                 // tiles x 4 KB operand A
-    unsigned char *bs = xs + (size_t)a.tiles * kTileBytes;        // d x 512 B operand B
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(bs + (size_t)a.d * kBBytes);
+    const int N = a.N, F = N / 8, d = a.d;
+    // shared memory: two raw staging slots (vector + factors), operand A, operand B, barrier
+    float *raw0 = reinterpret_cast<float *>(smem_raw);
+    float *fraw0 = raw0 + N;
+    float *raw1 = fraw0 + d * 64;
+    float *fraw1 = raw1 + N;
+    unsigned char *xs = reinterpret_cast<unsigned char *>(fraw1 + d * 64);  // tiles x 4 KB
+    unsigned char *bs = xs + (size_t)a.tiles * kTileBytes;                  // d x 512 B
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(bs + (size_t)d * kBBytes);
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int N = a.N, F = N / 8, d = a.d;
 
     long long e = (long long)blockIdx.x * a.entries_per_cta;
     const long long e_end = min(e + (long long)a.entries_per_cta, a.nb);
     if (e >= e_end) return;
 
-    // zero both operands once: padding rows of B (8..15) and, for BF16, the K 8..15 half of A stay zero
+    // operands zeroed once: padding rows of B (8..15) and, for BF16, the K 8..15 half of A stay zero
     for (int v = tid; v < (a.tiles * kTileBytes + d * kBBytes) / 16; v += kTcThreads)
-        reinterpret_cast<int4 *>(smem_raw)[v] = make_int4(0, 0, 0, 0);
+        reinterpret_cast<int4 *>(xs)[v] = make_int4(0, 0, 0, 0);
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                      "r"(a.tmem_cols)
@@ -174,51 +217,77 @@ template <int KIND> __global__ void __launch_bounds__(kTcThreads) fwd_tc_kernel(
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    TcPtrs nxt;
+    tc_load_ptrs(nxt, a, e, tid);
+    tc_stage_async(raw0, fraw0, nxt, a, tid);
+    if (e + 1 < e_end) tc_load_ptrs(nxt, a, e + 1, tid);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
+    const uint32_t tacc = tmem + 16u * a.tiles;  // run accumulator: one 16-column block per tile
     const uint32_t mbar_a = smem_u32(mbar);
     const uint32_t xs_a = smem_u32(xs), bs_a = smem_u32(bs);
     uint32_t phase = 0;
     bool failed = false;
-
-    constexpr int MAXT = 4;  // tiles per entry held in registers (N <= 4096)
-    float acc[MAXT][8];  // a run of entries is summed in FP32; FP64 only in the output atomics
     double *cur = nullptr;
+    constexpr int MAXT = 4;  // tiles per entry (N <= 4096)
 
-    for (; e < e_end && !failed; ++e) {
-        const float *x = a.in[e];
+    // run sum (TMEM accumulator) -> FP64 atomics into `dst`
+    auto flush = [&](double *dst) {
+        float v[MAXT][8];
+#pragma unroll
+        for (int t = 0; t < MAXT; ++t)
+            if (t < a.tiles) tmem_ld8(tacc + ((uint32_t)(warp * 32) << 16) + 16u * t, v[t]);
+        tmem_wait_ld();
+#pragma unroll
+        for (int t = 0; t < MAXT; ++t) {
+            const int c = t * kTileRows + warp * 32 + lane;
+            if (t < a.tiles && c < F)
+#pragma unroll
+                for (int r = 0; r < 8; ++r) atomicAdd(dst + c + r * F, (double)v[t][r]);
+        }
+    };
+
+    for (int slot = 0; e < e_end; ++e, slot ^= 1) {
+        float *raw = slot ? raw1 : raw0, *fraw = slot ? fraw1 : fraw0;
         double *o = a.out[e];
-        // factors: B_i[row r][k] = A_i(r, k), rows 8..15 stay zero
-        const float *const *mats = a.mats + e * d;
+        cp_async_wait_all();
+        __syncthreads();  // slot complete for every thread; the previous entry's MMAs are done
+        if (e + 1 < e_end) {
+            tc_stage_async(slot ? raw0 : raw1, slot ? fraw0 : fraw1, nxt, a, tid);
+            if (e + 2 < e_end) tc_load_ptrs(nxt, a, e + 2, tid);
+        }
+        // operands: B_i[row r][k] = A_i(r, k); input natural index p = k + 8c -> A row c, column k
         for (int v = tid; v < d * 64; v += kTcThreads) {
-            const int i = v >> 6, r = (v >> 3) & 7, k = v & 7;
-            put<KIND>(bs + (size_t)i * kBBytes, r, k, mats[i][r + (size_t)k * a.stride]);
+            const int i = v >> 6, r = v & 7, k = (v >> 3) & 7;
+            put<KIND>(bs + (size_t)i * kBBytes, r, k, fraw[v]);
         }
-        // input: natural index p = k + 8c -> operand row c, column k
-        if ((reinterpret_cast<uintptr_t>(x) & 15u) == 0) {
-            for (int q = tid; q < N / 4; q += kTcThreads) {
-                const float4 v4 = __ldcs(reinterpret_cast<const float4 *>(x) + q);
-                const uint32_t c = q >> 1, k0 = (q & 1) * 4;
-                put<KIND>(xs, c, k0 + 0, v4.x);
-                put<KIND>(xs, c, k0 + 1, v4.y);
-                put<KIND>(xs, c, k0 + 2, v4.z);
-                put<KIND>(xs, c, k0 + 3, v4.w);
-            }
-        } else {
-            for (int p = tid; p < N; p += kTcThreads) put<KIND>(xs, p >> 3, p & 7, __ldcs(x + p));
+        for (int q = tid; q < N / 4; q += kTcThreads) {
+            const float4 v4 = *reinterpret_cast<const float4 *>(raw + 4 * q);
+            const uint32_t c = q >> 1, k0 = (q & 1) * 4;
+            put<KIND>(xs, c, k0 + 0, v4.x);
+            put<KIND>(xs, c, k0 + 1, v4.y);
+            put<KIND>(xs, c, k0 + 2, v4.z);
+            put<KIND>(xs, c, k0 + 3, v4.w);
         }
+        // the run continues when this entry adds into the same output as the previous one;
+        // otherwise the previous run's sum leaves TMEM before the last mode overwrites it
+        const bool cont = (o == cur);
+        if (!cont && cur != nullptr) flush(cur);
+        cur = o;
         fence_async_smem();
         tc_fence_before();
         __syncthreads();
 
-        float v[MAXT][8];
         for (int i = d - 1; i >= 0; --i) {
             if (tid == 0) {
                 tc_fence_after();
+                const uint32_t dst = i > 0 ? tmem : tacc;
+                const uint32_t accumulate = (i == 0 && cont) ? 1u : 0u;
                 for (int t = 0; t < a.tiles; ++t)
-                    mma<KIND>(tmem + 16u * t, smem_desc(xs_a + t * kTileBytes), smem_desc(bs_a + i * kBBytes), 0u);
+                    mma<KIND>(dst + 16u * t, smem_desc(xs_a + t * kTileBytes), smem_desc(bs_a + i * kBBytes),
+                              accumulate);
                 mma_commit(mbar_a);
             }
             const bool ok = mbar_wait(mbar_a, phase);
@@ -230,11 +299,12 @@ template <int KIND> __global__ void __launch_bounds__(kTcThreads) fwd_tc_kernel(
             }
             phase ^= 1u;
             tc_fence_after();
-#pragma unroll
-            for (int t = 0; t < MAXT; ++t)
-                if (t < a.tiles) tmem_ld8(tmem + ((uint32_t)(warp * 32) << 16) + 16u * t, v[t]);
-            tmem_wait_ld();
             if (i > 0) {
+                float v[MAXT][8];
+#pragma unroll
+                for (int t = 0; t < MAXT; ++t)
+                    if (t < a.tiles) tmem_ld8(tmem + ((uint32_t)(warp * 32) << 16) + 16u * t, v[t]);
+                tmem_wait_ld();
                 // mode output element (row c, r) goes to natural position p = c + r*F,
                 // which is operand row p/8, column p%8 of the next mode
 #pragma unroll
@@ -249,43 +319,14 @@ template <int KIND> __global__ void __launch_bounds__(kTcThreads) fwd_tc_kernel(
                     }
                 }
                 fence_async_smem();
+                tc_fence_before();
+                __syncthreads();
             }
-            tc_fence_before();
-            __syncthreads();
         }
         if (failed) break;
-        // v[t][r] is element c + r*F of kron(A) . x
-        if (o != cur) {
-            if (cur != nullptr) {
-#pragma unroll
-                for (int t = 0; t < MAXT; ++t) {
-                    const int c = t * kTileRows + warp * 32 + lane;
-                    if (t < a.tiles && c < F)
-#pragma unroll
-                        for (int r = 0; r < 8; ++r) atomicAdd(cur + c + r * F, (double)acc[t][r]);
-                }
-            }
-            cur = o;
-#pragma unroll
-            for (int t = 0; t < MAXT; ++t)
-#pragma unroll
-                for (int r = 0; r < 8; ++r) acc[t][r] = v[t][r];
-        } else {
-#pragma unroll
-            for (int t = 0; t < MAXT; ++t)
-#pragma unroll
-                for (int r = 0; r < 8; ++r) acc[t][r] += v[t][r];
-        }
     }
-    if (cur != nullptr && !failed) {
-#pragma unroll
-        for (int t = 0; t < MAXT; ++t) {
-            const int c = t * kTileRows + warp * 32 + lane;
-            if (t < a.tiles && c < F)
-#pragma unroll
-                for (int r = 0; r < 8; ++r) atomicAdd(cur + c + r * F, (double)acc[t][r]);
-        }
-    }
+    cp_async_wait_all();
+    if (cur != nullptr && !failed) flush(cur);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -315,9 +356,10 @@ int launch_tc_forward(int kind, int d, int n, const float *const *mats, int stri
     const int F = a.N / 8;
     a.tiles = (F + kTileRows - 1) / kTileRows;
     int cols = 32;
-    while (cols < 16 * a.tiles) cols *= 2;
+    while (cols < 2 * 16 * a.tiles) cols *= 2;  // mode output + run accumulator
     a.tmem_cols = cols;
-    const size_t need = (size_t)a.tiles * kTileBytes + (size_t)d * kBBytes + 16;
+    const size_t need = (size_t)2 * (a.N + d * 64) * sizeof(float) + (size_t)a.tiles * kTileBytes +
+                        (size_t)d * kBBytes + 16;
     // resident CTAs per SM are limited so that their tensor-memory columns fit in 512:
     // each CTA reserves at least 1/max_ctas of the SM's shared memory
     const int max_ctas = 512 / cols;
