@@ -371,12 +371,10 @@ int launch_tc_forward(int kind, int d, int n, const float *const *mats, int stri
     const void *fn = kind == KRONMULT_COMPUTE_TF32 ? (const void *)fwd_tc_kernel<KIND_TF32>
                                                    : (const void *)fwd_tc_kernel<KIND_BF16>;
     if (!ensure_smem_attr(fn, smem)) return cudaErrorInvalidValue;
-    int occ = occupancy(fn, kTcThreads, smem);
-    if (occ < 1) return cudaErrorNotSupported;
-    if (occ > max_ctas) occ = max_ctas;
-    if (tune && tune->ctas_per_sm > 0 && tune->ctas_per_sm < occ) occ = tune->ctas_per_sm;
-    const long long ctas = (long long)di.sms * occ;
-    long long ept = (tune && tune->entries_per_team > 0) ? tune->entries_per_team : (nb + ctas - 1) / ctas;
+    // runs of 8 consecutive entries per CTA (the fan-in of a typical output group) and as
+    // many CTAs as that gives: the hardware keeps as many resident as the shared-memory
+    // reservation above allows, and that reservation keeps their TMEM within 512 columns
+    long long ept = (tune && tune->entries_per_team > 0) ? tune->entries_per_team : 8;
     if (ept < 1) ept = 1;
     if (ept > INT_MAX) ept = INT_MAX;
     a.entries_per_cta = (int)ept;
