@@ -106,7 +106,8 @@ int kronmult_batched_f32_f64out_async(int matrix_count, int matrix_size, const f
  * where grad_output_batched[k] is the gradient of the output vector entry k adds
  * into.  Entries that share a factor must share its gradient pointer; the
  * additions are atomic.  Either gradient table may be NULL to skip it.
- * Supports 2 <= n <= 8 (cudaErrorNotSupported otherwise).
+ * Supports 2 <= n <= 16 with n^d small enough for one team's shared memory
+ * (cudaErrorNotSupported otherwise).
  */
 int kronmult_batched_adjoint_f64_async(int matrix_count, int matrix_size, const double *const *matrix_list_batched,
                                        int matrix_stride, const double *const *input_batched,

@@ -45,69 +45,61 @@ template <typename T> struct AdjArgs {
     int slices;             // split of the grad contraction over the team
 };
 
-// forward-style mode product (contract fastest index), src -> dst (distinct buffers)
-template <typename T, int NN, int QMAX>
-__device__ __forceinline__ void mode_fast(const T *__restrict__ src, T *__restrict__ dst, const T *M, int F,
-                                          const Team &tm)
+// Every phase maps threads to individual output elements (not to whole fibres), so
+// that all lanes of a warp have work for any n: with n = 6 and 32-thread teams a
+// fibre mapping would leave 28 of 32 lanes idle in every second pass, and the FP64
+// pipe is charged per warp instruction.
+
+// forward-style mode product (contract the fastest index), src -> dst:
+// dst[c + r*F] = sum_k A(r, k) src[k + c*n]
+template <typename T>
+__device__ __forceinline__ void mode_fast_elem(const T *__restrict__ src, T *__restrict__ dst, const T *M, int n,
+                                               int N, const Team &tm)
 {
-#pragma unroll
-    for (int q = 0; q < QMAX; ++q) {
-        const int c = tm.rank + q * tm.size;
-        if (c < F) {
-            T xv[NN];
-            load_fibre<T, NN>(src + c * NN, xv);
-#pragma unroll
-            for (int r = 0; r < NN; ++r) {
-                T s = T(0);
-#pragma unroll
-                for (int k = 0; k < NN; ++k) s = fma_t<T>(M[r + k * NN], xv[k], s);
-                dst[c + r * F] = s;
-            }
-        }
+    const int F = N / n;
+    for (int p = tm.rank; p < N; p += tm.size) {
+        const int r = p / F, c = p - r * F;
+        const T *x = src + c * n;
+        T s = T(0);
+#pragma unroll 8
+        for (int k = 0; k < n; ++k) s = fma_t<T>(M[r + k * n], x[k], s);
+        dst[p] = s;
     }
 }
 
 // transposed mode product contracting the slowest index, in place through registers:
 // Z[r + n*t] = sum_k A(k, r) Q[t + R*k]
-template <typename T, int NN, int QMAX>
-__device__ __forceinline__ void mode_slow_inplace(T *buf, const T *M, int R, const Team &tm)
+template <typename T, int EMAX>
+__device__ __forceinline__ void mode_slow_elem(T *buf, const T *M, int n, int N, const Team &tm)
 {
-    T z[QMAX][NN];
+    const int R = N / n;
+    T z[EMAX];
 #pragma unroll
-    for (int q = 0; q < QMAX; ++q) {
-        const int t = tm.rank + q * tm.size;
-        if (t < R) {
-            T qv[NN];
-#pragma unroll
-            for (int k = 0; k < NN; ++k) qv[k] = buf[t + R * k];
-#pragma unroll
-            for (int r = 0; r < NN; ++r) {
-                T s = T(0);
-#pragma unroll
-                for (int k = 0; k < NN; ++k) s = fma_t<T>(M[k + r * NN], qv[k], s);
-                z[q][r] = s;
-            }
+    for (int j = 0; j < EMAX; ++j) {
+        const int p = tm.rank + j * tm.size;
+        if (p < N) {
+            const int t = p / n, r = p - t * n;
+            T s = T(0);
+#pragma unroll 8
+            for (int k = 0; k < n; ++k) s = fma_t<T>(M[k + r * n], buf[t + R * k], s);
+            z[j] = s;
         }
     }
     tm.sync();
 #pragma unroll
-    for (int q = 0; q < QMAX; ++q) {
-        const int t = tm.rank + q * tm.size;
-        if (t < R) {
-#pragma unroll
-            for (int r = 0; r < NN; ++r) buf[r + NN * t] = z[q][r];
-        }
+    for (int j = 0; j < EMAX; ++j) {
+        const int p = tm.rank + j * tm.size;
+        if (p < N) buf[p] = z[j];
     }
     tm.sync();
 }
 
-template <typename T, int NN, int QMAX>
-__global__ void __launch_bounds__(512) adj_smem_kernel(const AdjArgs<T> a)
+template <typename T, int EMAX>
+__global__ void __launch_bounds__(512) adj_elem_kernel(const AdjArgs<T> a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const Team tm(a.team_size);
-    constexpr int P = NN * NN;
-    const int N = a.N, d = a.d, R = N / NN;
+    const int n = a.n, N = a.N, d = a.d, R = N / n, P = n * n;
     T *base = reinterpret_cast<T *>(smem_raw) + (size_t)tm.id * a.team_elems;
     // slice layout: [p buffers][q][fac d*P][gacc d*P][gpart slices*P][cur grad pointers d]
     const int np = a.store_all ? d : 3;
@@ -140,7 +132,7 @@ __global__ void __launch_bounds__(512) adj_smem_kernel(const AdjArgs<T> a)
                 T *cp = curp[i];
                 if (gp != cp) {
                     if (cp != nullptr) {
-                        const int r = pr % NN, c = pr / NN;
+                        const int r = pr % n, c = pr / n;
                         atomic_add<T>(cp + r + (size_t)c * a.gstride, gacc[v]);
                     }
                     gacc[v] = T(0);
@@ -149,15 +141,21 @@ __global__ void __launch_bounds__(512) adj_smem_kernel(const AdjArgs<T> a)
             tm.sync();
             for (int v = tm.rank; v < d; v += tm.size) curp[v] = a.gmats[e * d + v];
         }
-        // stage x (as p_{d-1}), g, and the factors
+        // stage x (as p_{d-1}), g, and the factors fac[i*P + r + k*n] = A_i(r, k)
         T *xbuf = a.store_all ? pb + (size_t)(d - 1) * a.npad : pb;
         stage_vector(xbuf, a.in[e], N, tm);
         stage_vector(qb, a.gout[e], N, tm);
-        stage_factors<T, NN>(fac, a.mats + e * d, d, a.stride, tm);
+        {
+            const T *const *mats = a.mats + e * d;
+            for (int idx = tm.rank; idx < d * P; idx += tm.size) {
+                const int i = idx / P, rem = idx - i * P, k = rem / n, r = rem - k * n;
+                fac[idx] = mats[i][r + (size_t)k * a.stride];
+            }
+        }
         tm.sync();
         if (a.store_all) {
             for (int i = d - 1; i >= 1; --i) {
-                mode_fast<T, NN, QMAX>(pb + (size_t)i * a.npad, pb + (size_t)(i - 1) * a.npad, fac + i * P, R, tm);
+                mode_fast_elem<T>(pb + (size_t)i * a.npad, pb + (size_t)(i - 1) * a.npad, fac + i * P, n, N, tm);
                 tm.sync();
             }
         }
@@ -171,22 +169,22 @@ __global__ void __launch_bounds__(512) adj_smem_kernel(const AdjArgs<T> a)
                     const T *src = pb;
                     T *dst = pb + a.npad;
                     for (int m = d - 1; m > i; --m) {
-                        mode_fast<T, NN, QMAX>(src, dst, fac + m * P, R, tm);
+                        mode_fast_elem<T>(src, dst, fac + m * P, n, N, tm);
                         tm.sync();
                         src = dst;
                         dst = (dst == pb + a.npad) ? pb + 2 * (size_t)a.npad : pb + a.npad;
                     }
                     pi = src;
                 }
-                // partial G_(i) P_(i)^T over slices of t
+                // partial G_(i) P_(i)^T over slices of t: items (pair, slice)
                 const int S = a.slices;
                 const int tlen = (R + S - 1) / S;
                 for (int w = tm.rank; w < S * P; w += tm.size) {
                     const int pr = w % P, sl = w / P;
-                    const int r = pr % NN, c = pr / NN;
+                    const int r = pr % n, c = pr / n;
                     const int t0 = sl * tlen, t1 = min(R, t0 + tlen);
                     T s = T(0);
-                    for (int t = t0; t < t1; ++t) s = fma_t<T>(qb[t + R * r], pi[c + NN * t], s);
+                    for (int t = t0; t < t1; ++t) s = fma_t<T>(qb[t + R * r], pi[c + n * t], s);
                     gpart[w] = s;
                 }
                 tm.sync();
@@ -196,7 +194,7 @@ __global__ void __launch_bounds__(512) adj_smem_kernel(const AdjArgs<T> a)
                     gacc[i * P + pr] += s;
                 }
             }
-            if (i < d - 1 || want_gin) mode_slow_inplace<T, NN, QMAX>(qb, fac + i * P, R, tm);
+            if (i < d - 1 || want_gin) mode_slow_elem<T, EMAX>(qb, fac + i * P, n, N, tm);
         }
         if (want_gin) {
             T *gi = a.gin[e];
@@ -210,7 +208,7 @@ __global__ void __launch_bounds__(512) adj_smem_kernel(const AdjArgs<T> a)
             const int i = v / P, pr = v - i * P;
             T *cp = curp[i];
             if (cp != nullptr) {
-                const int r = pr % NN, c = pr / NN;
+                const int r = pr % n, c = pr / n;
                 atomic_add<T>(cp + r + (size_t)c * a.gstride, gacc[v]);
             }
         }
@@ -218,36 +216,20 @@ __global__ void __launch_bounds__(512) adj_smem_kernel(const AdjArgs<T> a)
 }
 
 template <typename T> using AdjFn = void (*)(const AdjArgs<T>);
-template <typename T> AdjFn<T> adj_lookup(int nn, int qmax);
+template <typename T> AdjFn<T> adj_lookup(int emax);
 
 }  // namespace kgb
 
 #define KGB_ADJ_INSTANTIATE(T)                                                                         \
     namespace kgb {                                                                                    \
-    template <> AdjFn<T> adj_lookup<T>(int nn, int qmax)                                               \
+    template <> AdjFn<T> adj_lookup<T>(int emax)                                                       \
     {                                                                                                  \
-        switch (nn * 16 + qmax) {                                                                      \
-        case 2 * 16 + 1: return adj_smem_kernel<T, 2, 1>;                                              \
-        case 2 * 16 + 2: return adj_smem_kernel<T, 2, 2>;                                              \
-        case 2 * 16 + 4: return adj_smem_kernel<T, 2, 4>;                                              \
-        case 3 * 16 + 1: return adj_smem_kernel<T, 3, 1>;                                              \
-        case 3 * 16 + 2: return adj_smem_kernel<T, 3, 2>;                                              \
-        case 3 * 16 + 4: return adj_smem_kernel<T, 3, 4>;                                              \
-        case 4 * 16 + 1: return adj_smem_kernel<T, 4, 1>;                                              \
-        case 4 * 16 + 2: return adj_smem_kernel<T, 4, 2>;                                              \
-        case 4 * 16 + 4: return adj_smem_kernel<T, 4, 4>;                                              \
-        case 5 * 16 + 1: return adj_smem_kernel<T, 5, 1>;                                              \
-        case 5 * 16 + 2: return adj_smem_kernel<T, 5, 2>;                                              \
-        case 5 * 16 + 4: return adj_smem_kernel<T, 5, 4>;                                              \
-        case 6 * 16 + 1: return adj_smem_kernel<T, 6, 1>;                                              \
-        case 6 * 16 + 2: return adj_smem_kernel<T, 6, 2>;                                              \
-        case 6 * 16 + 4: return adj_smem_kernel<T, 6, 4>;                                              \
-        case 7 * 16 + 1: return adj_smem_kernel<T, 7, 1>;                                              \
-        case 7 * 16 + 2: return adj_smem_kernel<T, 7, 2>;                                              \
-        case 7 * 16 + 4: return adj_smem_kernel<T, 7, 4>;                                              \
-        case 8 * 16 + 1: return adj_smem_kernel<T, 8, 1>;                                              \
-        case 8 * 16 + 2: return adj_smem_kernel<T, 8, 2>;                                              \
-        case 8 * 16 + 4: return adj_smem_kernel<T, 8, 4>;                                              \
+        switch (emax) {                                                                                \
+        case 1: return adj_elem_kernel<T, 1>;                                                          \
+        case 2: return adj_elem_kernel<T, 2>;                                                          \
+        case 4: return adj_elem_kernel<T, 4>;                                                          \
+        case 8: return adj_elem_kernel<T, 8>;                                                          \
+        case 16: return adj_elem_kernel<T, 16>;                                                        \
         default: return nullptr;                                                                       \
         }                                                                                              \
     }                                                                                                  \

@@ -89,28 +89,48 @@ static int adjoint_async(int d, int n, const T *const *mats, int stride, const T
     if (Nl > (long long)INT_MAX) return cudaErrorInvalidValue;
     if (nb == 0 || n == 0 || (!gin && !gmats)) return cudaSuccess;
     if (!mats || !in || !gout) return cudaErrorInvalidValue;
-    if (n < 2 || n > 8 || d < 1) return cudaErrorNotSupported;
+    if (n < 2 || n > 16 || d < 1) return cudaErrorNotSupported;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return cudaErrorInvalidDevice;
     const DeviceInfo &di = device_info(dev);
     const int N = (int)Nl, R = N / n, P = n * n;
-    int ts = 8;
+    // element-mapped phases: pick the team whose lanes are best used over N outputs
+    // (at most 16 outputs per thread); among equally good teams the largest wins
+    int ts = 0;
     if (tune && tune->team_size > 0) {
         ts = tune->team_size;
+        if (ts < 8 || ts > 512 || (ts & (ts - 1))) return cudaErrorInvalidValue;
+        while (ts < 512 && (N + ts - 1) / ts > 16) ts *= 2;
     } else {
-        while (ts < 512 && ts * 2 < R) ts *= 2;
+        double best = -1.0;
+        for (int c = 8; c <= 512; c *= 2) {
+            const int per = (N + c - 1) / c;
+            if (per > 16) continue;
+            const double util = (double)N / ((double)per * c);
+            if (util >= best - 0.02) {
+                if (util > best) best = util;
+                ts = c;
+            }
+            if (c >= N) break;
+        }
     }
-    if (ts < 8 || ts > 512 || (ts & (ts - 1))) return cudaErrorInvalidValue;
-    while (ts < 512 && (R + ts - 1) / ts > 4) ts *= 2;  // a requested team too small for 4 fibres/thread grows
-    const int q = (R + ts - 1) / ts;
-    int qmax = 1;
-    while (qmax < q) qmax *= 2;
-    if (qmax > 4) return cudaErrorNotSupported;
-    auto fn = adj_lookup<T>(n, qmax);
+    if (ts == 0) return cudaErrorNotSupported;
+    const int per = (N + ts - 1) / ts;
+    int emax = 1;
+    while (emax < per) emax *= 2;
+    if (emax > 16) return cudaErrorNotSupported;
+    auto fn = adj_lookup<T>(emax);
     if (!fn) return cudaErrorNotSupported;
     const int align = 16 / (int)sizeof(T);
     const int npad = round_up(N, align);
-    int slices = ts / P;
+    // gradient contraction items (pair, slice): slices * P a multiple of the team size
+    int g = P, h = ts;
+    while (h) {
+        const int t = g % h;
+        g = h;
+        h = t;
+    }
+    int slices = ts / g;
     if (slices < 1) slices = 1;
     if (slices > R) slices = R;
     auto team_elems_for = [&](int store_all) {

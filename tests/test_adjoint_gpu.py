@@ -71,7 +71,8 @@ def test_grad_input_golden_c5(cuda):
     assert O.rel_l2(gin, z["expected_grad_input_f64"]) <= 1e-13
 
 
-@pytest.mark.parametrize("d,n", [(1, 2), (2, 8), (3, 6), (4, 4), (6, 3), (3, 5), (2, 7), (5, 2), (6, 4)])
+@pytest.mark.parametrize("d,n", [(1, 2), (2, 8), (3, 6), (4, 4), (6, 3), (3, 5), (2, 7), (5, 2), (6, 4), (2, 9),
+                                 (2, 12), (3, 3)])
 def test_adjoint_shapes_f64(cuda, d, n):
     from kronmult_gb300 import workloads as W
 
