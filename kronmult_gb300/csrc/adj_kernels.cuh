@@ -215,8 +215,184 @@ __global__ void __launch_bounds__(512) adj_elem_kernel(const AdjArgs<T> a)
     }
 }
 
+// ---- fibre-mapped variant (compile-time n): each thread owns whole fibres and keeps
+// them in registers; used for FP32, where register reuse matters more than idle lanes
+
+// forward-style mode product (contract fastest index), src -> dst (distinct buffers)
+template <typename T, int NN, int QMAX>
+__device__ __forceinline__ void mode_fast(const T *__restrict__ src, T *__restrict__ dst, const T *M, int F,
+                                          const Team &tm)
+{
+#pragma unroll
+    for (int q = 0; q < QMAX; ++q) {
+        const int c = tm.rank + q * tm.size;
+        if (c < F) {
+            T xv[NN];
+            load_fibre<T, NN>(src + c * NN, xv);
+#pragma unroll
+            for (int r = 0; r < NN; ++r) {
+                T s = T(0);
+#pragma unroll
+                for (int k = 0; k < NN; ++k) s = fma_t<T>(M[r + k * NN], xv[k], s);
+                dst[c + r * F] = s;
+            }
+        }
+    }
+}
+
+// transposed mode product contracting the slowest index, in place through registers:
+// Z[r + n*t] = sum_k A(k, r) Q[t + R*k]
+template <typename T, int NN, int QMAX>
+__device__ __forceinline__ void mode_slow_inplace(T *buf, const T *M, int R, const Team &tm)
+{
+    T z[QMAX][NN];
+#pragma unroll
+    for (int q = 0; q < QMAX; ++q) {
+        const int t = tm.rank + q * tm.size;
+        if (t < R) {
+            T qv[NN];
+#pragma unroll
+            for (int k = 0; k < NN; ++k) qv[k] = buf[t + R * k];
+#pragma unroll
+            for (int r = 0; r < NN; ++r) {
+                T s = T(0);
+#pragma unroll
+                for (int k = 0; k < NN; ++k) s = fma_t<T>(M[k + r * NN], qv[k], s);
+                z[q][r] = s;
+            }
+        }
+    }
+    tm.sync();
+#pragma unroll
+    for (int q = 0; q < QMAX; ++q) {
+        const int t = tm.rank + q * tm.size;
+        if (t < R) {
+#pragma unroll
+            for (int r = 0; r < NN; ++r) buf[r + NN * t] = z[q][r];
+        }
+    }
+    tm.sync();
+}
+
+template <typename T, int NN, int QMAX>
+__global__ void __launch_bounds__(512) adj_smem_kernel(const AdjArgs<T> a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const Team tm(a.team_size);
+    constexpr int P = NN * NN;
+    const int N = a.N, d = a.d, R = N / NN;
+    T *base = reinterpret_cast<T *>(smem_raw) + (size_t)tm.id * a.team_elems;
+    // slice layout: [p buffers][q][fac d*P][gacc d*P][gpart slices*P][cur grad pointers d]
+    const int np = a.store_all ? d : 3;
+    T *pb = base;
+    T *qb = pb + (size_t)np * a.npad;
+    T *fac = qb + a.npad;
+    T *gacc = fac + d * P;
+    T *gpart = gacc + d * P;
+    T **curp = reinterpret_cast<T **>(gpart + a.slices * P + ((a.slices * P) & 1));
+    const bool want_gin = a.gin != nullptr;
+    const bool want_gA = a.gmats != nullptr;
+
+    const long long team_global = (long long)blockIdx.x * a.teams_per_cta + tm.id;
+    long long e = team_global * a.entries_per_team;
+    const long long e_end = min(e + (long long)a.entries_per_team, a.nb);
+    if (e >= e_end) return;
+
+    if (want_gA) {
+        for (int v = tm.rank; v < d * P; v += tm.size) gacc[v] = T(0);
+        for (int v = tm.rank; v < d; v += tm.size) curp[v] = nullptr;
+    }
+    tm.sync();
+
+    for (; e < e_end; ++e) {
+        // flush grad accumulators whose target changes with this entry
+        if (want_gA) {
+            for (int v = tm.rank; v < d * P; v += tm.size) {
+                const int i = v / P, pr = v - i * P;
+                T *gp = a.gmats[e * d + i];
+                T *cp = curp[i];
+                if (gp != cp) {
+                    if (cp != nullptr) {
+                        const int r = pr % NN, c = pr / NN;
+                        atomic_add<T>(cp + r + (size_t)c * a.gstride, gacc[v]);
+                    }
+                    gacc[v] = T(0);
+                }
+            }
+            tm.sync();
+            for (int v = tm.rank; v < d; v += tm.size) curp[v] = a.gmats[e * d + v];
+        }
+        // stage x (as p_{d-1}), g, and the factors
+        T *xbuf = a.store_all ? pb + (size_t)(d - 1) * a.npad : pb;
+        stage_vector(xbuf, a.in[e], N, tm);
+        stage_vector(qb, a.gout[e], N, tm);
+        stage_factors<T, NN>(fac, a.mats + e * d, d, a.stride, tm);
+        tm.sync();
+        if (a.store_all) {
+            for (int i = d - 1; i >= 1; --i) {
+                mode_fast<T, NN, QMAX>(pb + (size_t)i * a.npad, pb + (size_t)(i - 1) * a.npad, fac + i * P, R, tm);
+                tm.sync();
+            }
+        }
+        for (int i = 0; i < d; ++i) {
+            if (want_gA) {
+                const T *pi;
+                if (a.store_all) {
+                    pi = pb + (size_t)i * a.npad;
+                } else {
+                    // rebuild p_i = modes d-1..i+1 applied to x, ping-ponging pb[1] and pb[2]
+                    const T *src = pb;
+                    T *dst = pb + a.npad;
+                    for (int m = d - 1; m > i; --m) {
+                        mode_fast<T, NN, QMAX>(src, dst, fac + m * P, R, tm);
+                        tm.sync();
+                        src = dst;
+                        dst = (dst == pb + a.npad) ? pb + 2 * (size_t)a.npad : pb + a.npad;
+                    }
+                    pi = src;
+                }
+                // partial G_(i) P_(i)^T over slices of t
+                const int S = a.slices;
+                const int tlen = (R + S - 1) / S;
+                for (int w = tm.rank; w < S * P; w += tm.size) {
+                    const int pr = w % P, sl = w / P;
+                    const int r = pr % NN, c = pr / NN;
+                    const int t0 = sl * tlen, t1 = min(R, t0 + tlen);
+                    T s = T(0);
+                    for (int t = t0; t < t1; ++t) s = fma_t<T>(qb[t + R * r], pi[c + NN * t], s);
+                    gpart[w] = s;
+                }
+                tm.sync();
+                for (int pr = tm.rank; pr < P; pr += tm.size) {
+                    T s = T(0);
+                    for (int sl = 0; sl < S; ++sl) s += gpart[sl * P + pr];
+                    gacc[i * P + pr] += s;
+                }
+            }
+            if (i < d - 1 || want_gin) mode_slow_inplace<T, NN, QMAX>(qb, fac + i * P, R, tm);
+        }
+        if (want_gin) {
+            T *gi = a.gin[e];
+            for (int v = tm.rank; v < N; v += tm.size) atomic_add<T>(gi + v, qb[v]);
+        }
+        tm.sync();
+    }
+    if (want_gA) {
+        tm.sync();
+        for (int v = tm.rank; v < d * P; v += tm.size) {
+            const int i = v / P, pr = v - i * P;
+            T *cp = curp[i];
+            if (cp != nullptr) {
+                const int r = pr % NN, c = pr / NN;
+                atomic_add<T>(cp + r + (size_t)c * a.gstride, gacc[v]);
+            }
+        }
+    }
+}
+
 template <typename T> using AdjFn = void (*)(const AdjArgs<T>);
 template <typename T> AdjFn<T> adj_lookup(int emax);
+template <typename T> AdjFn<T> adj_fibre_lookup(int nn, int qmax);
 
 }  // namespace kgb
 
@@ -230,6 +406,38 @@ template <typename T> AdjFn<T> adj_lookup(int emax);
         case 4: return adj_elem_kernel<T, 4>;                                                          \
         case 8: return adj_elem_kernel<T, 8>;                                                          \
         case 16: return adj_elem_kernel<T, 16>;                                                        \
+        default: return nullptr;                                                                       \
+        }                                                                                              \
+    }                                                                                                  \
+    }
+
+// fibre-mapped adjoint instantiations (used for FP32)
+#define KGB_ADJ_FIBRE_INSTANTIATE(T)                                                                   \
+    namespace kgb {                                                                                    \
+    template <> AdjFn<T> adj_fibre_lookup<T>(int nn, int qmax)                                         \
+    {                                                                                                  \
+        switch (nn * 16 + qmax) {                                                                      \
+        case 2 * 16 + 1: return adj_smem_kernel<T, 2, 1>;                                              \
+        case 2 * 16 + 2: return adj_smem_kernel<T, 2, 2>;                                              \
+        case 2 * 16 + 4: return adj_smem_kernel<T, 2, 4>;                                              \
+        case 3 * 16 + 1: return adj_smem_kernel<T, 3, 1>;                                              \
+        case 3 * 16 + 2: return adj_smem_kernel<T, 3, 2>;                                              \
+        case 3 * 16 + 4: return adj_smem_kernel<T, 3, 4>;                                              \
+        case 4 * 16 + 1: return adj_smem_kernel<T, 4, 1>;                                              \
+        case 4 * 16 + 2: return adj_smem_kernel<T, 4, 2>;                                              \
+        case 4 * 16 + 4: return adj_smem_kernel<T, 4, 4>;                                              \
+        case 5 * 16 + 1: return adj_smem_kernel<T, 5, 1>;                                              \
+        case 5 * 16 + 2: return adj_smem_kernel<T, 5, 2>;                                              \
+        case 5 * 16 + 4: return adj_smem_kernel<T, 5, 4>;                                              \
+        case 6 * 16 + 1: return adj_smem_kernel<T, 6, 1>;                                              \
+        case 6 * 16 + 2: return adj_smem_kernel<T, 6, 2>;                                              \
+        case 6 * 16 + 4: return adj_smem_kernel<T, 6, 4>;                                              \
+        case 7 * 16 + 1: return adj_smem_kernel<T, 7, 1>;                                              \
+        case 7 * 16 + 2: return adj_smem_kernel<T, 7, 2>;                                              \
+        case 7 * 16 + 4: return adj_smem_kernel<T, 7, 4>;                                              \
+        case 8 * 16 + 1: return adj_smem_kernel<T, 8, 1>;                                              \
+        case 8 * 16 + 2: return adj_smem_kernel<T, 8, 2>;                                              \
+        case 8 * 16 + 4: return adj_smem_kernel<T, 8, 4>;                                              \
         default: return nullptr;                                                                       \
         }                                                                                              \
     }                                                                                                  \

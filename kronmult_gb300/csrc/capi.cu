@@ -94,45 +94,66 @@ static int adjoint_async(int d, int n, const T *const *mats, int stride, const T
     if (cudaGetDevice(&dev) != cudaSuccess) return cudaErrorInvalidDevice;
     const DeviceInfo &di = device_info(dev);
     const int N = (int)Nl, R = N / n, P = n * n;
-    // element-mapped phases: pick the team whose lanes are best used over N outputs
-    // (at most 16 outputs per thread); among equally good teams the largest wins
     int ts = 0;
-    if (tune && tune->team_size > 0) {
-        ts = tune->team_size;
-        if (ts < 8 || ts > 512 || (ts & (ts - 1))) return cudaErrorInvalidValue;
-        while (ts < 512 && (N + ts - 1) / ts > 16) ts *= 2;
-    } else {
-        double best = -1.0;
-        for (int c = 8; c <= 512; c *= 2) {
-            const int per = (N + c - 1) / c;
-            if (per > 16) continue;
-            const double util = (double)N / ((double)per * c);
-            if (util >= best - 0.02) {
-                if (util > best) best = util;
-                ts = c;
-            }
-            if (c >= N) break;
+    AdjFn<T> fn = nullptr;
+    int slices = 1;
+    if (sizeof(T) == 4 && n <= 8) {
+        // FP32: fibre-mapped kernel (whole fibres in registers, compile-time n)
+        ts = 8;
+        if (tune && tune->team_size > 0) {
+            ts = tune->team_size;
+            if (ts < 8 || ts > 512 || (ts & (ts - 1))) return cudaErrorInvalidValue;
+        } else {
+            while (ts < 512 && ts * 2 < R) ts *= 2;
         }
+        while (ts < 512 && (R + ts - 1) / ts > 4) ts *= 2;
+        const int q = (R + ts - 1) / ts;
+        int qmax = 1;
+        while (qmax < q) qmax *= 2;
+        if (qmax <= 4) fn = adj_fibre_lookup<T>(n, qmax);
+        slices = ts / P;
     }
-    if (ts == 0) return cudaErrorNotSupported;
-    const int per = (N + ts - 1) / ts;
-    int emax = 1;
-    while (emax < per) emax *= 2;
-    if (emax > 16) return cudaErrorNotSupported;
-    auto fn = adj_lookup<T>(emax);
-    if (!fn) return cudaErrorNotSupported;
-    const int align = 16 / (int)sizeof(T);
-    const int npad = round_up(N, align);
-    // gradient contraction items (pair, slice): slices * P a multiple of the team size
-    int g = P, h = ts;
-    while (h) {
-        const int t = g % h;
-        g = h;
-        h = t;
+    if (!fn) {
+        // element-mapped phases: pick the team whose lanes are best used over N outputs
+        // (at most 16 outputs per thread); among equally good teams the largest wins
+        ts = 0;
+        if (tune && tune->team_size > 0) {
+            ts = tune->team_size;
+            if (ts < 8 || ts > 512 || (ts & (ts - 1))) return cudaErrorInvalidValue;
+            while (ts < 512 && (N + ts - 1) / ts > 16) ts *= 2;
+        } else {
+            double best = -1.0;
+            for (int c = 8; c <= 512; c *= 2) {
+                const int per = (N + c - 1) / c;
+                if (per > 16) continue;
+                const double util = (double)N / ((double)per * c);
+                if (util >= best - 0.02) {
+                    if (util > best) best = util;
+                    ts = c;
+                }
+                if (c >= N) break;
+            }
+        }
+        if (ts == 0) return cudaErrorNotSupported;
+        const int per = (N + ts - 1) / ts;
+        int emax = 1;
+        while (emax < per) emax *= 2;
+        if (emax > 16) return cudaErrorNotSupported;
+        fn = adj_lookup<T>(emax);
+        if (!fn) return cudaErrorNotSupported;
+        // gradient contraction items (pair, slice): slices * P a multiple of the team size
+        int g = P, h = ts;
+        while (h) {
+            const int t = g % h;
+            g = h;
+            h = t;
+        }
+        slices = ts / g;
     }
-    int slices = ts / g;
     if (slices < 1) slices = 1;
     if (slices > R) slices = R;
+    const int align = 16 / (int)sizeof(T);
+    const int npad = round_up(N, align);
     auto team_elems_for = [&](int store_all) {
         const int np = store_all ? d : 3;
         const int ptr_elems = (8 * d + (int)sizeof(T) - 1) / (int)sizeof(T);

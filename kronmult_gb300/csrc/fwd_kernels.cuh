@@ -354,6 +354,63 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) fwd_single_kernel
     }
 }
 
+// One entry per team with output elements (not whole fibres) mapped to threads,
+// runtime n: every lane has work for any n.  Selected for FP64 when the fibre
+// mapping would leave more than a tenth of the lanes idle (for example n = 6:
+// 36 fibres per mode on 32-lane teams), since the FP64 pipe is charged per warp
+// instruction whatever the number of active lanes.
+template <typename T, typename TO, int EMAX>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) fwd_single_elem_kernel(const FwdArgs<T, TO> a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const Team tm(a.team_size);
+    T *buf = reinterpret_cast<T *>(smem_raw) + (size_t)tm.id * a.team_elems;
+    T *fac = buf + a.vec_pad;
+    const long long e = (long long)blockIdx.x * a.teams_per_cta + tm.id;
+    if (e >= a.nb) return;
+    const int n = a.n, N = a.N, F = N / n, P = n * n;
+    stage_vector(buf, a.in[e], N, tm);
+    {
+        const T *const *mats = a.mats + e * a.d;
+        for (int idx = tm.rank; idx < a.d * P; idx += tm.size) {
+            const int i = idx / P, rem = idx - i * P, k = rem / n, r = rem - k * n;
+            fac[idx] = mats[i][r + (size_t)k * a.stride];
+        }
+    }
+    tm.sync();
+    T y[EMAX];
+    for (int i = a.d - 1; i >= 0; --i) {
+        const T *M = fac + i * P;
+#pragma unroll
+        for (int j = 0; j < EMAX; ++j) {
+            const int p = tm.rank + j * tm.size;
+            if (p < N) {
+                const int r = p / F, c = p - r * F;
+                const T *x = buf + c * n;
+                T s = T(0);
+#pragma unroll 8
+                for (int k = 0; k < n; ++k) s = fma_t<T>(M[r + k * n], x[k], s);
+                y[j] = s;
+            }
+        }
+        if (i > 0) {
+            tm.sync();
+#pragma unroll
+            for (int j = 0; j < EMAX; ++j) {
+                const int p = tm.rank + j * tm.size;
+                if (p < N) buf[p] = y[j];
+            }
+            tm.sync();
+        }
+    }
+    TO *o = a.out[e];
+#pragma unroll
+    for (int j = 0; j < EMAX; ++j) {
+        const int p = tm.rank + j * tm.size;
+        if (p < N) atomic_add<TO>(o + p, (TO)y[j]);
+    }
+}
+
 // ---- generic kernel (runtime n, any N) ------------------------------------
 //
 // One CTA per entry (grid-stride over entries), one thread per output element.
@@ -409,6 +466,7 @@ __global__ void __launch_bounds__(256) fwd_generic_kernel(const FwdArgs<T, TO> a
 template <typename T, typename TO> using FwdSmemFn = void (*)(const FwdArgs<T, TO>);
 template <typename T, typename TO> FwdSmemFn<T, TO> fwd_smem_lookup(int nn, int qmax);
 template <typename T, typename TO> FwdSmemFn<T, TO> fwd_single_lookup(int nn, int qmax);
+template <typename T, typename TO> FwdSmemFn<T, TO> fwd_single_elem_lookup(int emax);
 template <typename T, typename TO> void *fwd_generic_ptr();
 
 }  // namespace kgb
@@ -473,6 +531,17 @@ template <typename T, typename TO> void *fwd_generic_ptr();
         case 8 * 16 + 1: return fwd_single_kernel<T, TO, 8, 1>;                                        \
         case 8 * 16 + 2: return fwd_single_kernel<T, TO, 8, 2>;                                        \
         case 8 * 16 + 4: return fwd_single_kernel<T, TO, 8, 4>;                                        \
+        default: return nullptr;                                                                       \
+        }                                                                                              \
+    }                                                                                                  \
+    template <> FwdSmemFn<T, TO> fwd_single_elem_lookup<T, TO>(int emax)                              \
+    {                                                                                                  \
+        switch (emax) {                                                                                \
+        case 1: return fwd_single_elem_kernel<T, TO, 1>;                                               \
+        case 2: return fwd_single_elem_kernel<T, TO, 2>;                                               \
+        case 4: return fwd_single_elem_kernel<T, TO, 4>;                                               \
+        case 8: return fwd_single_elem_kernel<T, TO, 8>;                                               \
+        case 16: return fwd_single_elem_kernel<T, TO, 16>;                                             \
         default: return nullptr;                                                                       \
         }                                                                                              \
     }                                                                                                  \

@@ -123,9 +123,38 @@ int plan_forward(FwdPlan<T, TO> &pl, int d, int n, const T *const *mats, int str
             const int vpad = round_up(N, 16 / (int)sizeof(T));
             const int fpad = round_up(d * n * n, 16 / (int)sizeof(T));
             const int team_elems = vpad + fpad;
-            const int teams = 256 / ts;
-            const size_t smem = (size_t)teams * team_elems * sizeof(T);
+            int teams = 256 / ts;
             auto fn = fwd_single_lookup<T, TO>(n, qmax);
+            // whole fibres per thread leave (ts*qmax - F) of ts*qmax slots idle; when that
+            // is more than a tenth, map output elements to threads instead (FP64 only:
+            // for FP32 the fibre's register reuse is worth more)
+            const double fibre_util = (double)F / ((double)ts * ((F + ts - 1) / ts));
+            if (sizeof(T) == 8 && fibre_util < 0.9 && !(tune && tune->team_size > 0)) {
+                int best_ts = 0;
+                double best = -1.0;
+                for (int c = 8; c <= 256; c *= 2) {
+                    const int per = (N + c - 1) / c;
+                    if (per > 16) continue;
+                    const double util = (double)N / ((double)per * c);
+                    if (util >= best - 0.02) {
+                        if (util > best) best = util;
+                        best_ts = c;
+                    }
+                    if (c >= N) break;
+                }
+                if (best_ts > 0 && best > fibre_util) {
+                    const int per = (N + best_ts - 1) / best_ts;
+                    int emax = 1;
+                    while (emax < per) emax *= 2;
+                    auto fe = fwd_single_elem_lookup<T, TO>(emax);
+                    if (fe) {
+                        fn = fe;
+                        ts = best_ts;
+                        teams = 256 / ts;
+                    }
+                }
+            }
+            const size_t smem = (size_t)teams * team_elems * sizeof(T);
             if (fn && smem <= (size_t)di.max_smem_optin && ensure_smem_attr((const void *)fn, smem)) {
                 const long long grid = (nb + teams - 1) / teams;
                 if (grid <= INT_MAX) {

@@ -236,3 +236,13 @@ def test_fp32_two_modes_per_pass(cuda, n, d):
     assert O.rel_l2(got, O.forward(b)) <= TOL32
     got64o, _ = run(b, cuda, dtype=torch.float32, out_dtype=torch.float64)
     assert O.rel_l2(got64o, O.forward(b)) <= TOL32
+
+
+@pytest.mark.parametrize("d,n", [(3, 6), (2, 6), (6, 3), (3, 5), (2, 7), (4, 3)])
+def test_fp64_element_mapping(cuda, d, n):
+    """FP64 shapes whose fibre count leaves lanes idle take the element-mapped kernel."""
+    from kronmult_gb300 import workloads as W
+
+    b = W.make_batch(d, n, n + 1, 6, 5, seed=500 + 10 * d + n)
+    got, _ = run(b, cuda)
+    assert O.rel_l2(got, O.forward(b)) <= TOL64
