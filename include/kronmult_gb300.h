@@ -130,8 +130,8 @@ int kronmult_batched_adjoint_f32_async(int matrix_count, int matrix_size, const 
  * kernel that pulls the items from a device queue.  The run only enqueues a
  * memset and a kernel, so it can be captured in a CUDA graph.  Rebuild the plan
  * if the pointer tables change.  In the deterministic mode no output vector may
- * be shared between groups (cudaErrorInvalidValue).  Supports 2 <= n <= 8 with
- * n^d small enough for one team's shared memory (cudaErrorNotSupported otherwise).
+ * be shared between groups (cudaErrorInvalidValue).  Supports 2 <= n <= 16 with
+ * n^d <= 2048 (FP64) or 4096 (FP32) (cudaErrorNotSupported otherwise).
  */
 typedef struct kronmult_group {
     int matrix_count, matrix_size, matrix_stride, nb_batch;

@@ -274,6 +274,81 @@ __device__ __forceinline__ void team_forward(const T *const *mats, const T *cons
 }
 
 // FP32 variants are capped at 64 registers so that four 256-thread CTAs fit on an SM
+// Element-mapped team forward with run accumulation (runtime n): thread `rank`
+// owns output elements p = rank + j*team_size (j < EMAX) of every mode, so all lanes
+// have work for any (d, n).  Same run / deterministic semantics as team_forward.
+template <typename T, typename TO, int EMAX, bool DET>
+__device__ __forceinline__ void team_forward_elem(const T *const *mats, const T *const *in, TO *const *out,
+                                                  const long long *perm, int d, int n, int stride, int N,
+                                                  long long e_begin, long long e_end, T *buf, T *fac,
+                                                  const Team &tm)
+{
+    const int F = N / n, P = n * n;
+    T acc[EMAX];
+    TO *cur = nullptr;
+    auto flush = [&](TO *dst) {
+#pragma unroll
+        for (int j = 0; j < EMAX; ++j) {
+            const int p = tm.rank + j * tm.size;
+            if (p < N) {
+                if constexpr (DET) {
+                    dst[p] = dst[p] + (TO)acc[j];
+                } else {
+                    atomic_add<TO>(dst + p, (TO)acc[j]);
+                }
+            }
+        }
+    };
+    for (long long ei = e_begin; ei < e_end; ++ei) {
+        const long long e = perm ? perm[ei] : ei;
+        TO *o = out[e];
+        stage_vector(buf, in[e], N, tm);
+        {
+            const T *const *m = mats + e * d;
+            for (int idx = tm.rank; idx < d * P; idx += tm.size) {
+                const int i = idx / P, rem = idx - i * P, k = rem / n, r = rem - k * n;
+                fac[idx] = m[i][r + (size_t)k * stride];
+            }
+        }
+        tm.sync();
+        T y[EMAX];
+        for (int i = d - 1; i >= 0; --i) {
+            const T *M = fac + i * P;
+#pragma unroll
+            for (int j = 0; j < EMAX; ++j) {
+                const int p = tm.rank + j * tm.size;
+                if (p < N) {
+                    const int r = p / F, c = p - r * F;
+                    const T *x = buf + c * n;
+                    T s = T(0);
+#pragma unroll 8
+                    for (int k = 0; k < n; ++k) s = fma_t<T>(M[r + k * n], x[k], s);
+                    y[j] = s;
+                }
+            }
+            tm.sync();  // every read of buf (and fac) for this mode is done
+            if (i > 0) {
+#pragma unroll
+                for (int j = 0; j < EMAX; ++j) {
+                    const int p = tm.rank + j * tm.size;
+                    if (p < N) buf[p] = y[j];
+                }
+                tm.sync();
+            }
+        }
+        if (o != cur) {
+            if (cur != nullptr) flush(cur);
+            cur = o;
+#pragma unroll
+            for (int j = 0; j < EMAX; ++j) acc[j] = y[j];
+        } else {
+#pragma unroll
+            for (int j = 0; j < EMAX; ++j) acc[j] += y[j];
+        }
+    }
+    if (cur != nullptr) flush(cur);
+}
+
 template <typename T, typename TO, int NN, int QMAX>
 __global__ void __launch_bounds__(512, sizeof(T) == 4 ? 2 : 1) fwd_smem_kernel(const FwdArgs<T, TO> a)
 {

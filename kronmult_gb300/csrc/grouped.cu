@@ -25,6 +25,8 @@
 
 namespace kgb {
 
+// Every group runs the element-mapped team forward (runtime n): all lanes busy for
+// any (d, n), and one small register footprint for the whole persistent kernel.
 template <typename T, typename TO, bool DET>
 __device__ __forceinline__ void grouped_dispatch(const GroupDesc &g, long long b, long long e, T *buf, T *fac,
                                                  const Team &tm)
@@ -32,18 +34,17 @@ __device__ __forceinline__ void grouped_dispatch(const GroupDesc &g, long long b
     const T *const *mats = reinterpret_cast<const T *const *>(g.mats);
     const T *const *in = reinterpret_cast<const T *const *>(g.in);
     TO *const *out = reinterpret_cast<TO *const *>(g.out);
-#define KGB_G(NN, Q)                                                                                   \
-    case NN * 16 + Q:                                                                                  \
-        team_forward<T, TO, NN, Q, DET>(mats, in, out, g.perm, g.d, g.stride, g.N, b, e, buf, fac, tm); \
+#define KGB_G(EM)                                                                                      \
+    case EM:                                                                                           \
+        team_forward_elem<T, TO, EM, DET>(mats, in, out, g.perm, g.d, g.n, g.stride, g.N, b, e, buf, fac, tm); \
         break;
-    switch (g.n * 16 + g.qmax) {
-        KGB_G(2, 1) KGB_G(2, 2) KGB_G(2, 4)
-        KGB_G(3, 1) KGB_G(3, 2) KGB_G(3, 4)
-        KGB_G(4, 1) KGB_G(4, 2) KGB_G(4, 4)
-        KGB_G(5, 1) KGB_G(5, 2) KGB_G(5, 4)
-        KGB_G(6, 1) KGB_G(6, 2) KGB_G(6, 4)
-        KGB_G(7, 1) KGB_G(7, 2) KGB_G(7, 4)
-        KGB_G(8, 1) KGB_G(8, 2) KGB_G(8, 4)
+    switch (g.emax) {
+        KGB_G(1) KGB_G(2) KGB_G(4) KGB_G(8)
+    case 16:
+        // 16 FP64 outputs (plus their run sums) per thread would spill: FP32 only
+        if constexpr (sizeof(T) == 4)
+            team_forward_elem<T, TO, 16, DET>(mats, in, out, g.perm, g.d, g.n, g.stride, g.N, b, e, buf, fac, tm);
+        break;
     default: break;
     }
 #undef KGB_G
@@ -86,25 +87,32 @@ const void *grouped_kernel_ptr(int dtype, int mode)
                                                : (const void *)grouped_kernel<float, float, false>;
 }
 
+// Element mapping: the team whose lanes are best used over the N outputs of an
+// entry (at most 16 outputs per thread), the largest among equally good ones.
 static int team_shape(int d, int n, int elem, const kronmult_tuning *tune, int &ts, int &qmax, int &team_elems,
-                      int &vec_pad)
+                      int &vec_pad, int &emax)
 {
     const long long Nl = pow_ll(n, d);
-    if (n < 2 || n > 8 || d < 1 || Nl > (long long)INT_MAX) return cudaErrorNotSupported;
-    const int N = (int)Nl, F = N / n;
-    if (tune && tune->team_size > 0) {
-        ts = tune->team_size;
-    } else {
-        const int qtarget = (n <= 4) ? 4 : 2;
-        ts = 8;
-        while (ts < kGroupedBlock && ts * qtarget < F) ts *= 2;
+    if (n < 2 || n > 16 || d < 1 || Nl > (long long)INT_MAX) return cudaErrorNotSupported;
+    const int N = (int)Nl;
+    ts = 0;
+    double best = -1.0;
+    for (int c = 8; c <= kGroupedBlock; c *= 2) {
+        if (tune && tune->team_size > 0 && c != tune->team_size) continue;
+        const int per = (N + c - 1) / c;
+        if (per > (elem == 8 ? 8 : 16)) continue;
+        const double util = (double)N / ((double)per * c);
+        if (util >= best - 0.02) {
+            if (util > best) best = util;
+            ts = c;
+        }
+        if (c >= N) break;
     }
-    if (ts < 8 || ts > kGroupedBlock || (ts & (ts - 1))) return cudaErrorInvalidValue;
-    while (ts < kGroupedBlock && (F + ts - 1) / ts > 4) ts *= 2;  // a requested team too small grows
-    const int q = (F + ts - 1) / ts;
-    qmax = 1;
-    while (qmax < q) qmax *= 2;
-    if (qmax > 4) return cudaErrorNotSupported;
+    if (ts == 0) return cudaErrorNotSupported;
+    const int per = (N + ts - 1) / ts;
+    emax = 1;
+    while (emax < per) emax *= 2;
+    qmax = 0;
     vec_pad = round_up(N, 16 / elem);
     team_elems = vec_pad + round_up(d * n * n, 16 / elem);
     return cudaSuccess;
@@ -140,7 +148,7 @@ int grouped_plan_create(GroupedPlan *&out, const kronmult_group *groups, int n_g
     int rc = cudaSuccess;
 
     // first pass: shapes and shared memory, to size the persistent grid
-    std::vector<int> ts(n_groups), qmax(n_groups), te(n_groups), vp(n_groups), tpc(n_groups);
+    std::vector<int> ts(n_groups), qmax(n_groups), te(n_groups), vp(n_groups), tpc(n_groups), em(n_groups);
     for (int g = 0; g < n_groups && rc == cudaSuccess; ++g) {
         const kronmult_group &G = groups[g];
         if (G.matrix_count < 0 || G.matrix_size < 0 || G.nb_batch < 0 ||
@@ -160,7 +168,7 @@ int grouped_plan_create(GroupedPlan *&out, const kronmult_group *groups, int n_g
             ts[g] = 0;
             continue;
         }
-        rc = team_shape(G.matrix_count, G.matrix_size, elem, tp, ts[g], qmax[g], te[g], vp[g]);
+        rc = team_shape(G.matrix_count, G.matrix_size, elem, tp, ts[g], qmax[g], te[g], vp[g], em[g]);
         if (rc != cudaSuccess) break;
         tpc[g] = kGroupedBlock / ts[g];
         while ((size_t)tpc[g] * te[g] * elem > (size_t)di.max_smem_optin && tpc[g] > 1) tpc[g] /= 2;
@@ -198,6 +206,7 @@ int grouped_plan_create(GroupedPlan *&out, const kronmult_group *groups, int n_g
         gd.team_elems = te[g];
         gd.vec_pad = vp[g];
         gd.qmax = qmax[g];
+        gd.emax = em[g];
         perm_offset.push_back(-1);
         const long long nb = G.nb_batch;
         if (nb == 0 || G.matrix_size == 0) {

@@ -14,6 +14,7 @@ struct GroupDesc {
     const long long *perm;  // entry order (null = identity)
     int d, n, stride, N;
     int team_size, teams_per_cta, team_elems, vec_pad, qmax;
+    int emax;  // > 0: element-mapped team forward with this many outputs per thread
 };
 
 struct CtaItem {             // one queue item: `count` team ranges of one group
