@@ -57,13 +57,14 @@ __device__ __forceinline__ void mode_fast_elem(const T *__restrict__ src, T *__r
                                                int N, const Team &tm)
 {
     const int F = N / n;
-    for (int p = tm.rank; p < N; p += tm.size) {
-        const int r = p / F, c = p - r * F;
+    for (int q = tm.rank; q < N; q += tm.size) {
+        // row r = q % n of fibre c = q / n: lanes of one fibre read the same words
+        const int c = q / n, r = q - c * n;
         const T *x = src + c * n;
         T s = T(0);
 #pragma unroll 8
         for (int k = 0; k < n; ++k) s = fma_t<T>(M[r + k * n], x[k], s);
-        dst[p] = s;
+        dst[c + r * F] = s;
     }
 }
 

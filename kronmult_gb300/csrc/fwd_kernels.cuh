@@ -275,8 +275,11 @@ __device__ __forceinline__ void team_forward(const T *const *mats, const T *cons
 
 // FP32 variants are capped at 64 registers so that four 256-thread CTAs fit on an SM
 // Element-mapped team forward with run accumulation (runtime n): thread `rank`
-// owns output elements p = rank + j*team_size (j < EMAX) of every mode, so all lanes
-// have work for any (d, n).  Same run / deterministic semantics as team_forward.
+// owns output elements q = rank + j*team_size (j < EMAX) of every mode, so all lanes
+// have work for any (d, n).  Element q is row r = q % n of fibre c = q / n: lanes that
+// share a fibre read the same shared-memory words (broadcast), and only the one store
+// per output, to position c + r*F, is strided.  Same run / deterministic semantics as
+// team_forward.
 template <typename T, typename TO, int EMAX, bool DET>
 __device__ __forceinline__ void team_forward_elem(const T *const *mats, const T *const *in, TO *const *out,
                                                   const long long *perm, int d, int n, int stride, int N,
@@ -289,8 +292,9 @@ __device__ __forceinline__ void team_forward_elem(const T *const *mats, const T 
     auto flush = [&](TO *dst) {
 #pragma unroll
         for (int j = 0; j < EMAX; ++j) {
-            const int p = tm.rank + j * tm.size;
-            if (p < N) {
+            const int q = tm.rank + j * tm.size;
+            if (q < N) {
+                const int c = q / n, r = q - c * n, p = c + r * F;
                 if constexpr (DET) {
                     dst[p] = dst[p] + (TO)acc[j];
                 } else {
@@ -316,9 +320,9 @@ __device__ __forceinline__ void team_forward_elem(const T *const *mats, const T 
             const T *M = fac + i * P;
 #pragma unroll
             for (int j = 0; j < EMAX; ++j) {
-                const int p = tm.rank + j * tm.size;
-                if (p < N) {
-                    const int r = p / F, c = p - r * F;
+                const int q = tm.rank + j * tm.size;
+                if (q < N) {
+                    const int c = q / n, r = q - c * n;
                     const T *x = buf + c * n;
                     T s = T(0);
 #pragma unroll 8
@@ -330,8 +334,11 @@ __device__ __forceinline__ void team_forward_elem(const T *const *mats, const T 
             if (i > 0) {
 #pragma unroll
                 for (int j = 0; j < EMAX; ++j) {
-                    const int p = tm.rank + j * tm.size;
-                    if (p < N) buf[p] = y[j];
+                    const int q = tm.rank + j * tm.size;
+                    if (q < N) {
+                        const int c = q / n, r = q - c * n;
+                        buf[c + r * F] = y[j];
+                    }
                 }
                 tm.sync();
             }
@@ -458,9 +465,9 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) fwd_single_elem_k
         const T *M = fac + i * P;
 #pragma unroll
         for (int j = 0; j < EMAX; ++j) {
-            const int p = tm.rank + j * tm.size;
-            if (p < N) {
-                const int r = p / F, c = p - r * F;
+            const int q = tm.rank + j * tm.size;  // row r = q % n of fibre c = q / n
+            if (q < N) {
+                const int c = q / n, r = q - c * n;
                 const T *x = buf + c * n;
                 T s = T(0);
 #pragma unroll 8
@@ -472,8 +479,11 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) fwd_single_elem_k
             tm.sync();
 #pragma unroll
             for (int j = 0; j < EMAX; ++j) {
-                const int p = tm.rank + j * tm.size;
-                if (p < N) buf[p] = y[j];
+                const int q = tm.rank + j * tm.size;
+                if (q < N) {
+                    const int c = q / n, r = q - c * n;
+                    buf[c + r * F] = y[j];
+                }
             }
             tm.sync();
         }
@@ -481,8 +491,11 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) fwd_single_elem_k
     TO *o = a.out[e];
 #pragma unroll
     for (int j = 0; j < EMAX; ++j) {
-        const int p = tm.rank + j * tm.size;
-        if (p < N) atomic_add<TO>(o + p, (TO)y[j]);
+        const int q = tm.rank + j * tm.size;
+        if (q < N) {
+            const int c = q / n, r = q - c * n;
+            atomic_add<TO>(o + c + r * F, (TO)y[j]);
+        }
     }
 }
 
