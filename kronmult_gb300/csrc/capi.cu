@@ -116,24 +116,10 @@ static int adjoint_async(int d, int n, const T *const *mats, int stride, const T
     if (!fn) {
         // element-mapped phases: pick the team whose lanes are best used over N outputs
         // (at most 16 outputs per thread); among equally good teams the largest wins
-        ts = 0;
-        if (tune && tune->team_size > 0) {
-            ts = tune->team_size;
-            if (ts < 8 || ts > 512 || (ts & (ts - 1))) return cudaErrorInvalidValue;
-            while (ts < 512 && (N + ts - 1) / ts > 16) ts *= 2;
-        } else {
-            double best = -1.0;
-            for (int c = 8; c <= 512; c *= 2) {
-                const int per = (N + c - 1) / c;
-                if (per > 16) continue;
-                const double util = (double)N / ((double)per * c);
-                if (util >= best - 0.02) {
-                    if (util > best) best = util;
-                    ts = c;
-                }
-                if (c >= N) break;
-            }
-        }
+        if (tune && tune->team_size > 0 && (tune->team_size < 8 || tune->team_size > 512 ||
+                                             (tune->team_size & (tune->team_size - 1))))
+            return cudaErrorInvalidValue;
+        ts = elem_team_size(N, 16, tune && tune->team_size > 0 ? tune->team_size : 0, 512);
         if (ts == 0) return cudaErrorNotSupported;
         const int per = (N + ts - 1) / ts;
         int emax = 1;

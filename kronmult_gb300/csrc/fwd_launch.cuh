@@ -36,6 +36,39 @@ inline long long pow_ll(int b, int e)
 
 inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
 
+// Team size (power of two, 8..max_ts) for an element-mapped kernel over N outputs:
+// the best lane utilisation N / (ts * ceil(N / ts)) with at most max_per outputs per
+// thread; among teams within 2 % of the best, the one closest to 8 outputs per thread.
+// `forced` > 0 fixes the size (grown until max_per holds).  Returns 0 if none fits.
+inline int elem_team_size(int N, int max_per, int forced, int max_ts)
+{
+    if (forced > 0) {
+        int ts = forced;
+        while (ts < max_ts && (N + ts - 1) / ts > max_per) ts *= 2;
+        return (N + ts - 1) / ts <= max_per ? ts : 0;
+    }
+    double best = -1.0;
+    for (int c = 8; c <= max_ts; c *= 2) {
+        const int per = (N + c - 1) / c;
+        if (per <= max_per) {
+            const double u = (double)N / ((double)per * c);
+            if (u > best) best = u;
+        }
+    }
+    int ts = 0, dist = 1 << 30;
+    for (int c = 8; c <= max_ts; c *= 2) {
+        const int per = (N + c - 1) / c;
+        if (per > max_per) continue;
+        const double u = (double)N / ((double)per * c);
+        const int dd = per > 8 ? per - 8 : 8 - per;
+        if (u >= best - 0.02 && dd < dist) {
+            dist = dd;
+            ts = c;
+        }
+    }
+    return ts;
+}
+
 // largest power of two <= v (v >= 1)
 inline int pow2_floor(long long v)
 {
@@ -130,18 +163,9 @@ int plan_forward(FwdPlan<T, TO> &pl, int d, int n, const T *const *mats, int str
             // for FP32 the fibre's register reuse is worth more)
             const double fibre_util = (double)F / ((double)ts * ((F + ts - 1) / ts));
             if (sizeof(T) == 8 && fibre_util < 0.9 && !(tune && tune->team_size > 0)) {
-                int best_ts = 0;
-                double best = -1.0;
-                for (int c = 8; c <= 256; c *= 2) {
-                    const int per = (N + c - 1) / c;
-                    if (per > 16) continue;
-                    const double util = (double)N / ((double)per * c);
-                    if (util >= best - 0.02) {
-                        if (util > best) best = util;
-                        best_ts = c;
-                    }
-                    if (c >= N) break;
-                }
+                const int best_ts = elem_team_size(N, 16, 0, 256);
+                const double best =
+                    best_ts ? (double)N / ((double)best_ts * ((N + best_ts - 1) / best_ts)) : 0.0;
                 if (best_ts > 0 && best > fibre_util) {
                     const int per = (N + best_ts - 1) / best_ts;
                     int emax = 1;

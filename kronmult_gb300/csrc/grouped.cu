@@ -88,26 +88,15 @@ const void *grouped_kernel_ptr(int dtype, int mode)
 }
 
 // Element mapping: the team whose lanes are best used over the N outputs of an
-// entry (at most 16 outputs per thread), the largest among equally good ones.
+// entry; among equally good teams the one closest to 8 outputs per thread (enough
+// independent FMA chains per thread, few threads per barrier).
 static int team_shape(int d, int n, int elem, const kronmult_tuning *tune, int &ts, int &qmax, int &team_elems,
                       int &vec_pad, int &emax)
 {
     const long long Nl = pow_ll(n, d);
     if (n < 2 || n > 16 || d < 1 || Nl > (long long)INT_MAX) return cudaErrorNotSupported;
     const int N = (int)Nl;
-    ts = 0;
-    double best = -1.0;
-    for (int c = 8; c <= kGroupedBlock; c *= 2) {
-        if (tune && tune->team_size > 0 && c != tune->team_size) continue;
-        const int per = (N + c - 1) / c;
-        if (per > (elem == 8 ? 8 : 16)) continue;
-        const double util = (double)N / ((double)per * c);
-        if (util >= best - 0.02) {
-            if (util > best) best = util;
-            ts = c;
-        }
-        if (c >= N) break;
-    }
+    ts = elem_team_size(N, elem == 8 ? 8 : 16, tune && tune->team_size > 0 ? tune->team_size : 0, kGroupedBlock);
     if (ts == 0) return cudaErrorNotSupported;
     const int per = (N + ts - 1) / ts;
     emax = 1;
