@@ -356,6 +356,135 @@ __device__ __forceinline__ void team_forward_elem(const T *const *mats, const T 
     if (cur != nullptr) flush(cur);
 }
 
+// Element-mapped team forward with a fully asynchronous two-slot pipeline: while
+// entry e is computed, the copies of entry e+1's vector and factors are in flight
+// (cp.async), issued from pointers that were themselves copied into shared memory
+// (cp.async) one entry earlier, so no dependent global load sits on the critical
+// path.  Slot layout per team: [vec A][fac A][vec B][fac B][ptr A][ptr B] where a
+// pointer slot holds the entry's input pointer and its d factor pointers.
+template <typename T>
+__device__ __forceinline__ void elem_copy_ptrs(const T **pslot, const T *const *in, const T *const *mats,
+                                               long long e, int d, const Team &tm)
+{
+    for (int v = tm.rank; v <= d; v += tm.size) {
+        const void *src = v == 0 ? (const void *)(in + e) : (const void *)(mats + e * d + (v - 1));
+        cp_async<8>(pslot + v, src);
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void elem_copy_data(T *vec, T *fac, const T *const *pslot, int d, int n, int stride,
+                                               int N, const Team &tm)
+{
+    const T *src = pslot[0];
+    const size_t bytes = (size_t)N * sizeof(T);
+    if (((reinterpret_cast<uintptr_t>(src) & 15u) == 0) && ((bytes & 15u) == 0)) {
+        for (int v = tm.rank; v < (int)(bytes >> 4); v += tm.size)
+            cp_async<16>(reinterpret_cast<int4 *>(vec) + v, reinterpret_cast<const int4 *>(src) + v);
+    } else {
+        for (int v = tm.rank; v < N; v += tm.size) cp_async<(int)sizeof(T)>(vec + v, src + v);
+    }
+    const int P = n * n;
+    for (int idx = tm.rank; idx < d * P; idx += tm.size) {
+        const int i = idx / P, rem = idx - i * P, k = rem / n, r = rem - k * n;
+        cp_async<(int)sizeof(T)>(fac + idx, pslot[1 + i] + r + (size_t)k * stride);
+    }
+}
+
+template <typename T, typename TO, int EMAX, bool DET>
+__device__ __forceinline__ void team_forward_elem_pf(const T *const *mats, const T *const *in, TO *const *out,
+                                                     const long long *perm, int d, int n, int stride, int N,
+                                                     long long e_begin, long long e_end, T *slots, int slot_elems,
+                                                     const T **ptrs, const Team &tm)
+{
+    if (e_begin >= e_end) return;
+    const int F = N / n, P = n * n;
+    constexpr int kAlign = 16 / (int)sizeof(T);
+    const int vpad = (N + kAlign - 1) / kAlign * kAlign;  // factors follow the vector in a slot
+    auto vec = [&](int s) { return s ? slots + slot_elems : slots; };
+    auto fac = [&](int s) { return (s ? slots + slot_elems : slots) + vpad; };
+    auto pslot = [&](int s) { return s ? ptrs + (d + 1) : ptrs; };
+    auto entry = [&](long long ei) { return perm ? perm[ei] : ei; };
+
+    T acc[EMAX];
+    TO *cur = nullptr;
+    auto flush = [&](TO *dst) {
+#pragma unroll
+        for (int j = 0; j < EMAX; ++j) {
+            const int q = tm.rank + j * tm.size;
+            if (q < N) {
+                const int c = q / n, r = q - c * n, p = c + r * F;
+                if constexpr (DET) {
+                    dst[p] = dst[p] + (TO)acc[j];
+                } else {
+                    atomic_add<TO>(dst + p, (TO)acc[j]);
+                }
+            }
+        }
+    };
+
+    // prologue: pointers of the first entry (waited for), its data copy, pointers of the second
+    elem_copy_ptrs<T>(pslot(0), in, mats, entry(e_begin), d, tm);
+    cp_async_commit();
+    cp_async_wait_all();
+    tm.sync();
+    elem_copy_data<T>(vec(0), fac(0), pslot(0), d, n, stride, N, tm);
+    if (e_begin + 1 < e_end) elem_copy_ptrs<T>(pslot(1), in, mats, entry(e_begin + 1), d, tm);
+    cp_async_commit();
+
+    for (long long ei = e_begin; ei < e_end; ++ei) {
+        const int s = (int)((ei - e_begin) & 1);
+        TO *o = out[entry(ei)];
+        cp_async_wait_all();
+        tm.sync();  // data of ei and pointers of ei+1 are in shared memory for the whole team
+        if (ei + 1 < e_end) {
+            elem_copy_data<T>(vec(s ^ 1), fac(s ^ 1), pslot(s ^ 1), d, n, stride, N, tm);
+            if (ei + 2 < e_end) elem_copy_ptrs<T>(pslot(s), in, mats, entry(ei + 2), d, tm);
+        }
+        cp_async_commit();
+        T *buf = vec(s);
+        T y[EMAX];
+        for (int i = d - 1; i >= 0; --i) {
+            const T *M = fac(s) + i * P;
+#pragma unroll
+            for (int j = 0; j < EMAX; ++j) {
+                const int q = tm.rank + j * tm.size;
+                if (q < N) {
+                    const int c = q / n, r = q - c * n;
+                    const T *x = buf + c * n;
+                    T sum = T(0);
+#pragma unroll 8
+                    for (int k = 0; k < n; ++k) sum = fma_t<T>(M[r + k * n], x[k], sum);
+                    y[j] = sum;
+                }
+            }
+            tm.sync();  // every read of this slot for this mode is done
+            if (i > 0) {
+#pragma unroll
+                for (int j = 0; j < EMAX; ++j) {
+                    const int q = tm.rank + j * tm.size;
+                    if (q < N) {
+                        const int c = q / n, r = q - c * n;
+                        buf[c + r * F] = y[j];
+                    }
+                }
+                tm.sync();
+            }
+        }
+        if (o != cur) {
+            if (cur != nullptr) flush(cur);
+            cur = o;
+#pragma unroll
+            for (int j = 0; j < EMAX; ++j) acc[j] = y[j];
+        } else {
+#pragma unroll
+            for (int j = 0; j < EMAX; ++j) acc[j] += y[j];
+        }
+    }
+    if (cur != nullptr) flush(cur);
+    cp_async_wait_all();
+}
+
 template <typename T, typename TO, int NN, int QMAX>
 __global__ void __launch_bounds__(512, sizeof(T) == 4 ? 2 : 1) fwd_smem_kernel(const FwdArgs<T, TO> a)
 {

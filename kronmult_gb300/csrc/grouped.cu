@@ -28,22 +28,25 @@ namespace kgb {
 // Every group runs the element-mapped team forward (runtime n): all lanes busy for
 // any (d, n), and one small register footprint for the whole persistent kernel.
 template <typename T, typename TO, bool DET>
-__device__ __forceinline__ void grouped_dispatch(const GroupDesc &g, long long b, long long e, T *buf, T *fac,
+__device__ __forceinline__ void grouped_dispatch(const GroupDesc &g, long long b, long long e, T *slots,
                                                  const Team &tm)
 {
     const T *const *mats = reinterpret_cast<const T *const *>(g.mats);
     const T *const *in = reinterpret_cast<const T *const *>(g.in);
     TO *const *out = reinterpret_cast<TO *const *>(g.out);
+    const T **ptrs = reinterpret_cast<const T **>(slots + 2 * (size_t)g.vec_pad);
 #define KGB_G(EM)                                                                                      \
     case EM:                                                                                           \
-        team_forward_elem<T, TO, EM, DET>(mats, in, out, g.perm, g.d, g.n, g.stride, g.N, b, e, buf, fac, tm); \
+        team_forward_elem_pf<T, TO, EM, DET>(mats, in, out, g.perm, g.d, g.n, g.stride, g.N, b, e, slots,       \
+                                             g.vec_pad, ptrs, tm);                                      \
         break;
     switch (g.emax) {
         KGB_G(1) KGB_G(2) KGB_G(4) KGB_G(8)
     case 16:
         // 16 FP64 outputs (plus their run sums) per thread would spill: FP32 only
         if constexpr (sizeof(T) == 4)
-            team_forward_elem<T, TO, 16, DET>(mats, in, out, g.perm, g.d, g.n, g.stride, g.N, b, e, buf, fac, tm);
+            team_forward_elem_pf<T, TO, 16, DET>(mats, in, out, g.perm, g.d, g.n, g.stride, g.N, b, e, slots,
+                                                 g.vec_pad, ptrs, tm);
         break;
     default: break;
     }
@@ -68,9 +71,9 @@ __global__ void __launch_bounds__(kGroupedBlock, 2)
         const int team_id = threadIdx.x / g.team_size;
         if (team_id < ci.count) {
             const Team tm(g.team_size);
-            T *buf = reinterpret_cast<T *>(smem_raw) + (size_t)team_id * g.team_elems;
+            T *slots = reinterpret_cast<T *>(smem_raw) + (size_t)team_id * g.team_elems;
             const TeamRange r = ranges[ci.first_range + team_id];
-            grouped_dispatch<T, TO, DET>(g, r.begin, r.end, buf, buf + g.vec_pad, tm);
+            grouped_dispatch<T, TO, DET>(g, r.begin, r.end, slots, tm);
         }
         __syncthreads();
     }
@@ -102,8 +105,11 @@ static int team_shape(int d, int n, int elem, const kronmult_tuning *tune, int &
     emax = 1;
     while (emax < per) emax *= 2;
     qmax = 0;
-    vec_pad = round_up(N, 16 / elem);
-    team_elems = vec_pad + round_up(d * n * n, 16 / elem);
+    // two slots of [vector | factors] plus two pointer slots of d+1 pointers
+    const int align = 16 / elem;
+    const int slot = round_up(N, align) + round_up(d * n * n, align);
+    vec_pad = slot;  // elements per data slot
+    team_elems = 2 * slot + round_up(2 * (d + 1) * 8 / elem, align);
     return cudaSuccess;
 }
 
