@@ -224,6 +224,42 @@ def _timed(fn, stream, reps: int, warmup: int = 3) -> float:
     return e0.elapsed_time(e1) / reps
 
 
+def reference_gpu_ms(db, reps: int = 3, dtype: str = "f64"):
+    """Milliseconds per launch of the reference's own GPU kernel (built from the reference
+    sources into oracle/_ref) on the same batch, or None where it is not available.
+    The kernel overwrites its inputs, so each launch runs on a fresh copy made outside
+    the event-timed window."""
+    import torch
+
+    from oracle import ref_gpu
+
+    if not ref_gpu.available():
+        return None
+    x0 = db.inputs
+    x = x0.clone()
+    ws = torch.empty_like(x)
+    out = torch.zeros_like(db.outputs)
+    es = x.element_size()
+    k = torch.arange(db.nb, device=x.device, dtype=torch.int64)
+    in_ptrs = x.data_ptr() + k * (db.N * es)
+    ws_ptrs = ws.data_ptr() + k * (db.N * es)
+    out_ptrs = out.data_ptr() + db.out_index * (out.shape[1] * es)
+    st = torch.cuda.current_stream()
+    total = 0.0
+    for rep in range(reps + 1):
+        x.copy_(x0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        ref_gpu.launch(db.d, db.n, db.mat_ptrs.data_ptr(), db.stride, in_ptrs.data_ptr(), out_ptrs.data_ptr(),
+                       ws_ptrs.data_ptr(), db.nb, dtype=dtype, stream=st.cuda_stream)
+        e1.record(st)
+        torch.cuda.synchronize()
+        if rep > 0:
+            total += e0.elapsed_time(e1)
+    return total / reps
+
+
 def suite(args):
     """Every configuration, one JSON line each (diagnostic report, not the headline)."""
     import ctypes
@@ -271,6 +307,11 @@ def suite(args):
             tune = None if pf == 0 else {"prefetch": 1}
             ms = _timed(lambda: db.forward(stream=st, tuning=tune), st, reps)
             emit(f"{cname}_fwd_f64" + ("" if pf == 0 else "_single_slot"), b, ms, 8, 8)
+        ref = reference_gpu_ms(db, reps=3)
+        if ref is not None:
+            emit(f"{cname}_reference_gpu_kernel_f64", b, ref, 8, 8,
+                 {"note": "kronmult_gpu/kronmult.cu built for sm_103a; inputs restored between launches, "
+                          "outside the timed window"})
         if cname == "c2":
             ms = _timed(lambda: lib.kronmult_batched_f64_noalloc(b.d, b.n, db.mat_ptrs.data_ptr(), b.stride,
                                                                  db.in_ptrs.data_ptr(), db.out_ptrs.data_ptr(),
@@ -485,6 +526,20 @@ def main():
         roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                     "frac": achieved_gbs / hbm_peak, "traffic": traffic, "peak_source": hbm_src}
 
+    ref_gpu_line = None
+    if args.dtype == "f64":
+        try:
+            ref_ms = reference_gpu_ms(db, reps=3)
+        except Exception as exc:  # the comparator is optional; report why it is missing
+            ref_ms, ref_gpu_line = None, {"unavailable": str(exc)[:200]}
+        if ref_ms:
+            ref_gpu_line = {"value": flops_step / (ref_ms / 1e3) / 1e9, "unit": "GFLOP/s", "ms_per_launch": ref_ms,
+                            "speedup_of_ours": ref_ms / (per_launch_s * 1e3),
+                            "kernel": "kronmult_gpu/kronmult.cu cuda_kronmult_batchelement<double>, built for "
+                                      "sm_103a from the reference sources, same workload and GPU"}
+        elif ref_gpu_line is None:
+            ref_gpu_line = {"unavailable": "reference cubin not built (needs the reference sources)"}
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(b, np.float64 if args.dtype == "f64" else np.float32)
@@ -503,6 +558,7 @@ def main():
             "gbytes_per_s": achieved_gbs,
             "roofline": roofline,
             "cpu_baseline": cpu,
+            "reference_gpu_kernel": ref_gpu_line,
             "e2e": {"value": e2e_value, "unit": "GFLOP/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms},
             "gpu_launches": args.steps,
