@@ -260,6 +260,61 @@ def reference_gpu_ms(db, reps: int = 3, dtype: str = "f64"):
     return total / reps
 
 
+def suite_large(args, emit, reps):
+    """The reference's published 'large' case, on device-generated seeded data."""
+    import torch
+
+    from kronmult_gb300 import DeviceBatch
+    from kronmult_gb300.workloads import Batch
+
+    d, n, stride, nb, distinct = 6, 8, 67, 3903, 5
+    N = n ** d
+    nb = max(8, int(nb * args.scale))
+    dev = torch.device("cuda", 0)
+    g = torch.Generator(device=dev)
+    g.manual_seed(3903)
+    idx = torch.arange(nb, device=dev, dtype=torch.int64)
+    out_index = torch.where(idx < distinct, idx, (idx * distinct) // nb)  # tests/utils/utils_cpu.h:73-83
+    for dt, name in ((torch.float64, "f64"), (torch.float32, "f32")):
+        fac = (torch.rand((nb * d, n * stride), generator=g, device=dev, dtype=dt) * 2 - 1)
+        x0 = torch.randn((nb, N), generator=g, device=dev, dtype=dt)
+        outs = torch.zeros((distinct, N), device=dev, dtype=dt)
+        db = DeviceBatch(d, n, stride, fac, x0.clone(), outs, idx, out_index, with_workspace=True)
+        meta = Batch("large", d, n, stride, n * stride, np.zeros((1, 1)), np.zeros((nb, 0)), np.zeros((distinct, 0)),
+                     np.zeros(1, dtype=np.int64), np.zeros(nb, dtype=np.int64))
+        meta.inputs = np.empty((nb, 0))
+
+        class _Shape:  # flops/bytes of the full shape for emit()
+            def flops(self_):
+                return 2.0 * d * n * N * nb
+
+            def bytes(self_, i, o):
+                return i * N * nb + i * n * n * d * nb + 2.0 * o * N * distinct
+
+        st = torch.cuda.current_stream()
+        total = 0.0
+        for rep in range(reps + 1):
+            db.inputs.copy_(x0)  # the global-memory path overwrites inputs, as the reference does
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            db.forward(stream=st)
+            e1.record(st)
+            torch.cuda.synchronize()
+            if rep:
+                total += e0.elapsed_time(e1)
+        es = 8 if name == "f64" else 4
+        emit(f"large_n8_d6_b{nb}_{name}", _Shape(), total / reps, es, es,
+             {"published_v100_ms": 221 if name == "f64" else 100, "source": "tests/bench_results.txt:12,42"})
+        if name == "f64":
+            db.inputs.copy_(x0)
+            ref = reference_gpu_ms(db, reps=1)
+            if ref is not None:
+                emit(f"large_n8_d6_b{nb}_reference_gpu_kernel_f64", _Shape(), ref, 8, 8)
+        del db, fac, x0, outs
+        torch.cuda.empty_cache()
+
+
 def suite(args):
     """Every configuration, one JSON line each (diagnostic report, not the headline)."""
     import ctypes
@@ -365,6 +420,12 @@ def suite(args):
         emit(f"c4_fwd_{cname}", b, ms, 4, 8, {"rel_l2_vs_fp64": O.rel_l2(got, ref), "max_err_vs_fp64": O.max_rel(got, ref)})
     del db
     torch.cuda.empty_cache()
+
+    # the reference's own published benchmark shape ("large": n=8, d=6, N=262144, 3903
+    # entries, matrix_stride 67, 5 distinct outputs reached through its aliasing pattern,
+    # tests/bench_results.txt:4): vectors beyond shared memory, global-memory sweep
+    if want("large"):
+        suite_large(args, emit, reps)
 
     # C5: forward + adjoint; plain FP64 launches vs FP32 captured in one CUDA graph
     if not want("c5"):

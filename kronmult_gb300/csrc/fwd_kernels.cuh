@@ -628,6 +628,72 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) fwd_single_elem_k
     }
 }
 
+// ---- large vectors: global-memory sweep (compile-time n) -------------------
+//
+// For n^d beyond one SM's shared memory (the reference's large benchmark: n = 8,
+// d = 6, N = 262144) the sweep streams through the caller's `input` and
+// `workspace` vectors, which it overwrites as the reference does
+// (kronmult_gpu/kronmult.cu:119-121).  One CTA per entry; every thread handles whole
+// fibres (16-byte vector loads of a fibre, n outputs per fibre in registers,
+// stores coalesced across the CTA); the factor of the current mode sits in shared
+// memory; the last mode adds straight into the output with atomics, so there is no
+// extra pass over the result.  In FP64 the FP64 pipe stays the bound: the HBM
+// traffic of 2N values per mode is an order of magnitude below its time.
+template <typename T, typename TO, int NN>
+__global__ void __launch_bounds__(256) fwd_global_kernel(const FwdArgs<T, TO> a)
+{
+    __shared__ T fac[NN * NN];
+    const int N = a.N, F = N / NN, d = a.d;
+    for (long long e = blockIdx.x; e < a.nb; e += gridDim.x) {
+        T *src = const_cast<T *>(a.in[e]);
+        T *dst = a.ws[e];
+        TO *o = a.out[e];
+        for (int i = d - 1; i >= 0; --i) {
+            const T *A = a.mats[e * d + i];
+            __syncthreads();  // previous mode finished with fac and with its src/dst
+            for (int v = threadIdx.x; v < NN * NN; v += blockDim.x) {
+                const int k = v / NN, r = v - k * NN;
+                fac[v] = A[r + (size_t)k * a.stride];
+            }
+            __syncthreads();
+            T m[NN * NN <= 16 ? NN * NN : 1];
+            if constexpr (NN * NN <= 16) {
+#pragma unroll
+                for (int j = 0; j < NN * NN; ++j) m[j] = fac[j];
+            }
+            for (int c = threadIdx.x; c < F; c += blockDim.x) {
+                T xv[NN];
+                const T *x = src + (size_t)c * NN;
+                if constexpr ((NN * sizeof(T)) % 16 == 0) {
+#pragma unroll
+                    for (int v = 0; v < (int)(NN * sizeof(T) / 16); ++v)
+                        *reinterpret_cast<int4 *>(&xv[v * 16 / sizeof(T)]) = reinterpret_cast<const int4 *>(x)[v];
+                } else {
+#pragma unroll
+                    for (int k = 0; k < NN; ++k) xv[k] = x[k];
+                }
+#pragma unroll
+                for (int r = 0; r < NN; ++r) {
+                    T s = T(0);
+#pragma unroll
+                    for (int k = 0; k < NN; ++k) {
+                        const T mv = (NN * NN <= 16) ? m[(NN * NN <= 16) ? r + k * NN : 0] : fac[r + k * NN];
+                        s = fma_t<T>(mv, xv[k], s);
+                    }
+                    if (i > 0) {
+                        dst[c + (size_t)r * F] = s;
+                    } else {
+                        atomic_add<TO>(o + c + (size_t)r * F, (TO)s);
+                    }
+                }
+            }
+            T *t = src;
+            src = dst;
+            dst = t;
+        }
+    }
+}
+
 // ---- generic kernel (runtime n, any N) ------------------------------------
 //
 // One CTA per entry (grid-stride over entries), one thread per output element.
@@ -684,6 +750,7 @@ template <typename T, typename TO> using FwdSmemFn = void (*)(const FwdArgs<T, T
 template <typename T, typename TO> FwdSmemFn<T, TO> fwd_smem_lookup(int nn, int qmax);
 template <typename T, typename TO> FwdSmemFn<T, TO> fwd_single_lookup(int nn, int qmax);
 template <typename T, typename TO> FwdSmemFn<T, TO> fwd_single_elem_lookup(int emax);
+template <typename T, typename TO> FwdSmemFn<T, TO> fwd_global_lookup(int nn);
 template <typename T, typename TO> void *fwd_generic_ptr();
 
 }  // namespace kgb
@@ -759,6 +826,19 @@ template <typename T, typename TO> void *fwd_generic_ptr();
         case 4: return fwd_single_elem_kernel<T, TO, 4>;                                               \
         case 8: return fwd_single_elem_kernel<T, TO, 8>;                                               \
         case 16: return fwd_single_elem_kernel<T, TO, 16>;                                             \
+        default: return nullptr;                                                                       \
+        }                                                                                              \
+    }                                                                                                  \
+    template <> FwdSmemFn<T, TO> fwd_global_lookup<T, TO>(int nn)                                     \
+    {                                                                                                  \
+        switch (nn) {                                                                                  \
+        case 2: return fwd_global_kernel<T, TO, 2>;                                                    \
+        case 3: return fwd_global_kernel<T, TO, 3>;                                                    \
+        case 4: return fwd_global_kernel<T, TO, 4>;                                                    \
+        case 5: return fwd_global_kernel<T, TO, 5>;                                                    \
+        case 6: return fwd_global_kernel<T, TO, 6>;                                                    \
+        case 7: return fwd_global_kernel<T, TO, 7>;                                                    \
+        case 8: return fwd_global_kernel<T, TO, 8>;                                                    \
         default: return nullptr;                                                                       \
         }                                                                                              \
     }                                                                                                  \

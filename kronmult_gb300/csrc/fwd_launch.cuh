@@ -295,6 +295,26 @@ int plan_forward(FwdPlan<T, TO> &pl, int d, int n, const T *const *mats, int str
         }
     }
 
+    // ---- large vectors through input/workspace in global memory (compile-time n)
+    if (n >= 2 && n <= 8 && d >= 1 && ws) {
+        const size_t smem_s = ((size_t)round_up(n * n, 2) + 2 * (size_t)round_up(N, 2)) * sizeof(T);
+        if (smem_s > (size_t)di.max_smem_optin) {
+            auto fn = fwd_global_lookup<T, TO>(n);
+            if (fn) {
+                int per_sm = occupancy((const void *)fn, 256, 0);
+                if (per_sm < 1) per_sm = 1;
+                long long grid = (long long)di.sms * per_sm;
+                if (grid > nb) grid = nb;
+                pl.fn = (const void *)fn;
+                pl.smem_path = true;  // same launch signature as the shared-memory kernels
+                pl.grid = dim3((unsigned)grid);
+                pl.block = dim3(256);
+                pl.smem = 0;
+                return cudaSuccess;
+            }
+        }
+    }
+
     // ---- generic path
     const void *fn = fwd_generic_ptr<T, TO>();
     const size_t smem_s = ((size_t)round_up(n * n, 2) + 2 * (size_t)round_up(N, 2)) * sizeof(T);

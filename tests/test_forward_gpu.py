@@ -246,3 +246,18 @@ def test_fp64_element_mapping(cuda, d, n):
     b = W.make_batch(d, n, n + 1, 6, 5, seed=500 + 10 * d + n)
     got, _ = run(b, cuda)
     assert O.rel_l2(got, O.forward(b)) <= TOL64
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_large_published_shape(cuda, dtype):
+    """The reference's published 'large' shape (n = 8, d = 6, N = 262144, stride 67,
+    its aliasing pattern onto 5 outputs) on 12 entries, through the global-memory path."""
+    from kronmult_gb300 import workloads as W
+
+    b = W.make_batch(6, 8, 67, 12, 1, seed=3903)
+    idx = np.arange(b.nb)
+    b = W.Batch(b.name, b.d, b.n, b.stride, b.block, b.factors, b.inputs, b.out_init[:5],
+                b.fac_index, np.where(idx < 5, idx, (idx * 5) // b.nb))
+    got, _ = run(b, cuda, dtype=dtype, ws=True)
+    tol = TOL64 if dtype == torch.float64 else TOL32
+    assert O.rel_l2(got, O.forward(b)) <= tol
