@@ -637,10 +637,11 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) fwd_single_elem_k
 // fibres (16-byte vector loads of a fibre, n outputs per fibre in registers,
 // stores coalesced across the CTA); the factor of the current mode sits in shared
 // memory; the last mode adds straight into the output with atomics, so there is no
-// extra pass over the result.  In FP64 the FP64 pipe stays the bound: the HBM
+// extra pass over the result.  One 512-thread CTA per entry, scheduled by the
+// hardware (no persistent tail).  In FP64 the FP64 pipe stays the bound: the HBM
 // traffic of 2N values per mode is an order of magnitude below its time.
 template <typename T, typename TO, int NN>
-__global__ void __launch_bounds__(256) fwd_global_kernel(const FwdArgs<T, TO> a)
+__global__ void __launch_bounds__(512) fwd_global_kernel(const FwdArgs<T, TO> a)
 {
     __shared__ T fac[NN * NN];
     const int N = a.N, F = N / NN, d = a.d;

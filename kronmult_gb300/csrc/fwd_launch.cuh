@@ -301,14 +301,11 @@ int plan_forward(FwdPlan<T, TO> &pl, int d, int n, const T *const *mats, int str
         if (smem_s > (size_t)di.max_smem_optin) {
             auto fn = fwd_global_lookup<T, TO>(n);
             if (fn) {
-                int per_sm = occupancy((const void *)fn, 256, 0);
-                if (per_sm < 1) per_sm = 1;
-                long long grid = (long long)di.sms * per_sm;
-                if (grid > nb) grid = nb;
+                const long long grid = nb < INT_MAX ? nb : INT_MAX;  // one CTA per entry
                 pl.fn = (const void *)fn;
                 pl.smem_path = true;  // same launch signature as the shared-memory kernels
                 pl.grid = dim3((unsigned)grid);
-                pl.block = dim3(256);
+                pl.block = dim3(512);
                 pl.smem = 0;
                 return cudaSuccess;
             }
