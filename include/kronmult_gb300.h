@@ -200,6 +200,20 @@ int kronmult_device_error(int *code, int clear);
  * reference counterpart).  Allocates and synchronises; not for use in a graph. */
 int kronmult_diag_fp64_fma_gflops(double *gflops);
 
+/*
+ * FP64-accurate forward in emulated arithmetic (no reference counterpart): FP64
+ * factors, inputs and outputs; every mode product in double-float (pairs of FP32,
+ * exact two-product and two-sum) on the FP32 pipe, which on GB300 is ~60x the FP64
+ * pipe.  Relative error a few units of 2^-47 per mode (the FP64 path's contract is
+ * 1e-13 relative L2).  Per entry and per factor power-of-two scaling keeps any finite
+ * input in range; values more than 2^126 below the largest of their vector or factor
+ * count as zero.  Same semantics as kronmult_batched_f64_async otherwise (inputs not
+ * modified).  Supports 2 <= n <= 8 with n^d fitting one team's shared memory.
+ */
+int kronmult_batched_f64_emulated_async(int matrix_count, int matrix_size, const double *const *matrix_list_batched,
+                                        int matrix_stride, const double *const *input_batched,
+                                        double *const *output_batched, int nb_batch, void *stream);
+
 /* Integer power as in the reference's pow_int (kronmult_gpu/kronmult.cuh:10), in 64 bits. */
 long long kronmult_pow_int(int number, int power);
 

@@ -261,3 +261,14 @@ def forward_from_host(b: DeviceBatch, h_inputs: torch.Tensor, h_factors: torch.T
         with torch.cuda.stream(s_out):
             h_outputs.copy_(b.outputs, non_blocking=True)
     return s_in, s_cmp, s_out
+
+
+def forward_f64_emulated(b: DeviceBatch, stream=None) -> None:
+    """FP64 batch forward computed in double-float arithmetic on the FP32 pipe
+    (kronmult_batched_f64_emulated_async): FP64-accurate (relative error ~1e-14)."""
+    if b.inputs.dtype != torch.float64 or b.outputs.dtype != torch.float64:
+        raise TypeError("the emulated FP64 forward needs float64 factors, inputs and outputs")
+    st = _lib.lib().kronmult_batched_f64_emulated_async(b.d, b.n, b.mat_ptrs.data_ptr(), b.stride,
+                                                         b.in_ptrs.data_ptr(), b.out_ptrs.data_ptr(), b.nb,
+                                                         _stream_handle(stream))
+    _lib.check(st, "kronmult_batched_f64_emulated_async")
