@@ -362,6 +362,19 @@ def suite(args):
             tune = None if pf == 0 else {"prefetch": 1}
             ms = _timed(lambda: db.forward(stream=st, tuning=tune), st, reps)
             emit(f"{cname}_fwd_f64" + ("" if pf == 0 else "_single_slot"), b, ms, 8, 8)
+        from kronmult_gb300.api import forward_f64_emulated
+
+        ms = _timed(lambda: forward_f64_emulated(db, stream=st), st, reps)
+        db.outputs.zero_()
+        db.forward(stream=st)
+        torch.cuda.synchronize()
+        ref_out = db.outputs.clone()
+        db.outputs.zero_()
+        forward_f64_emulated(db, stream=st)
+        torch.cuda.synchronize()
+        err = (torch.linalg.norm(db.outputs - ref_out) / torch.linalg.norm(ref_out)).item()
+        emit(f"{cname}_fwd_f64_emulated", b, ms, 8, 8, {"rel_l2_vs_native_fp64": err,
+                                                         "fp64_roof_multiple": b.flops() / ms / 1e6 / fp64_peak})
         ref = reference_gpu_ms(db, reps=3)
         if ref is not None:
             emit(f"{cname}_reference_gpu_kernel_f64", b, ref, 8, 8,
