@@ -365,12 +365,12 @@ def suite(args):
         from kronmult_gb300.api import forward_f64_emulated
 
         ms = _timed(lambda: forward_f64_emulated(db, stream=st), st, reps)
-        db.outputs.zero_()
-        db.forward(stream=st)
-        torch.cuda.synchronize()
-        ref_out = db.outputs.clone()
-        db.outputs.zero_()
-        forward_f64_emulated(db, stream=st)
+        with torch.cuda.stream(st):  # checks on the launch stream: zeroing ordered before the kernels
+            db.outputs.zero_()
+            db.forward(stream=st)
+            ref_out = db.outputs.clone()
+            db.outputs.zero_()
+            forward_f64_emulated(db, stream=st)
         torch.cuda.synchronize()
         err = (torch.linalg.norm(db.outputs - ref_out) / torch.linalg.norm(ref_out)).item()
         emit(f"{cname}_fwd_f64_emulated", b, ms, 8, 8, {"rel_l2_vs_native_fp64": err,
@@ -387,10 +387,11 @@ def suite(args):
             emit("c2_fwd_f64_noalloc", b, ms, 8, 8, launches=2)
             db32 = DeviceBatch.from_host(b, device=dev, dtype=torch.float32)
             ms = _timed(lambda: db32.forward(stream=st), st, reps)
-            db32.outputs.zero_()
-            db32.forward(stream=st)
-            db.outputs.zero_()
-            db.forward(stream=st)
+            with torch.cuda.stream(st):
+                db32.outputs.zero_()
+                db32.forward(stream=st)
+                db.outputs.zero_()
+                db.forward(stream=st)
             torch.cuda.synchronize()
             err = (torch.linalg.norm(db32.outputs.double() - db.outputs) / torch.linalg.norm(db.outputs)).item()
             emit("c2_fwd_f32", b, ms, 4, 4, {"rel_l2_vs_fp64": err})
@@ -426,8 +427,9 @@ def suite(args):
     db = DeviceBatch.from_host(b, device=dev, dtype=torch.float32, out_dtype=torch.float64) if modes4 else None
     for cname, code in modes4:
         ms = _timed(lambda: forward_f32_f64out(db, compute=code, stream=st), st, reps)
-        db.outputs.zero_()
-        forward_f32_f64out(db, compute=code, stream=st)
+        with torch.cuda.stream(st):
+            db.outputs.zero_()
+            forward_f32_f64out(db, compute=code, stream=st)
         torch.cuda.synchronize()
         got = db.outputs.cpu().numpy()
         emit(f"c4_fwd_{cname}", b, ms, 4, 8, {"rel_l2_vs_fp64": O.rel_l2(got, ref), "max_err_vs_fp64": O.max_rel(got, ref)})
@@ -466,8 +468,10 @@ def suite(args):
             ms = _timed(lambda: graph.replay(), torch.cuda.current_stream(), reps)
         else:
             ms = _timed(step, st, reps)
-        db.outputs.zero_(); gin.zero_(); gfa.zero_()
         with torch.cuda.stream(st):
+            db.outputs.zero_()
+            gin.zero_()
+            gfa.zero_()
             step()
         torch.cuda.synchronize()
         res[dt] = (ms, db.outputs.double().cpu().numpy(), gin.double().cpu().numpy(), gfa.double().cpu().numpy())
