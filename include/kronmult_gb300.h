@@ -214,6 +214,30 @@ int kronmult_batched_f64_emulated_async(int matrix_count, int matrix_size, const
                                         int matrix_stride, const double *const *input_batched,
                                         double *const *output_batched, int nb_batch, void *stream);
 
+/*
+ * Indexed forward: integer maps instead of pointer arrays (the interface form
+ * named as the next step after the drop-in; no reference counterpart).
+ *   entry k, mode i uses factor  factors + factor_index[k*d + i] * factor_pitch
+ *   entry k reads                inputs  + (input_index ? input_index[k] : k) * input_pitch
+ *   entry k adds into            outputs + output_index[k] * output_pitch
+ * (all element offsets; every array device-resident).  The pointer arrays of the
+ * kronmult_batched interface are built on `stream` into caller-provided `scratch`
+ * of at least kronmult_indexed_scratch_bytes(d, nb) bytes, then the regular forward
+ * runs; nothing is allocated or synchronised.  Inputs are not modified (vectors
+ * beyond shared memory are not supported here: cudaErrorNotSupported).
+ */
+long long kronmult_indexed_scratch_bytes(int matrix_count, int nb_batch);
+int kronmult_indexed_f64_async(int matrix_count, int matrix_size, int matrix_stride, const double *factors,
+                               long long factor_pitch, const int *factor_index, const double *inputs,
+                               long long input_pitch, const int *input_index, double *outputs,
+                               long long output_pitch, const int *output_index, int nb_batch, void *scratch,
+                               long long scratch_bytes, void *stream);
+int kronmult_indexed_f32_async(int matrix_count, int matrix_size, int matrix_stride, const float *factors,
+                               long long factor_pitch, const int *factor_index, const float *inputs,
+                               long long input_pitch, const int *input_index, float *outputs,
+                               long long output_pitch, const int *output_index, int nb_batch, void *scratch,
+                               long long scratch_bytes, void *stream);
+
 /* Integer power as in the reference's pow_int (kronmult_gpu/kronmult.cuh:10), in 64 bits. */
 long long kronmult_pow_int(int number, int power);
 

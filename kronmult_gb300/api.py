@@ -272,3 +272,31 @@ def forward_f64_emulated(b: DeviceBatch, stream=None) -> None:
                                                          b.in_ptrs.data_ptr(), b.out_ptrs.data_ptr(), b.nb,
                                                          _stream_handle(stream))
     _lib.check(st, "kronmult_batched_f64_emulated_async")
+
+
+def forward_indexed(d: int, n: int, stride: int, factors: torch.Tensor, factor_index: torch.Tensor,
+                    inputs: torch.Tensor, outputs: torch.Tensor, output_index: torch.Tensor,
+                    input_index: torch.Tensor | None = None, scratch: torch.Tensor | None = None,
+                    stream=None) -> torch.Tensor:
+    """Indexed forward (kronmult_indexed_*): factors (M, pitch) rows of factor storage,
+    factor_index (B, d) int32, inputs (B or I, N), outputs (E, N), output_index (B,) int32.
+    Returns the scratch tensor that holds the pointer tables (keep it alive until the
+    launch has run, or pass one in to reuse it)."""
+    dt = inputs.dtype
+    name = {torch.float64: "kronmult_indexed_f64_async", torch.float32: "kronmult_indexed_f32_async"}.get(dt)
+    if name is None:
+        raise TypeError("indexed forward is defined for float64 and float32")
+    nb = int(output_index.shape[0])
+    need = int(_lib.lib().kronmult_indexed_scratch_bytes(d, nb))
+    if scratch is None or scratch.numel() * scratch.element_size() < need:
+        scratch = torch.empty(max(need, 8), dtype=torch.uint8, device=inputs.device)
+    fi = factor_index.to(torch.int32).contiguous()
+    oi = output_index.to(torch.int32).contiguous()
+    ii = None if input_index is None else input_index.to(torch.int32).contiguous()
+    st = getattr(_lib.lib(), name)(d, n, stride, factors.data_ptr(), factors.shape[1], fi.data_ptr(),
+                                   inputs.data_ptr(), inputs.shape[1], None if ii is None else ii.data_ptr(),
+                                   outputs.data_ptr(), outputs.shape[1], oi.data_ptr(), nb, scratch.data_ptr(),
+                                   scratch.numel() * scratch.element_size(), _stream_handle(stream))
+    _lib.check(st, name)
+    scratch._kronmult_keep = (fi, oi, ii)
+    return scratch
