@@ -375,6 +375,15 @@ def suite(args):
         err = (torch.linalg.norm(db.outputs - ref_out) / torch.linalg.norm(ref_out)).item()
         emit(f"{cname}_fwd_f64_emulated", b, ms, 8, 8, {"rel_l2_vs_native_fp64": err,
                                                          "fp64_roof_multiple": b.flops() / ms / 1e6 / fp64_peak})
+        # indexed entry point: int32 maps in, pointer arrays expanded on the stream
+        from kronmult_gb300.api import forward_indexed
+
+        fidx = (db.fac_index[:, None] * b.d + torch.arange(b.d, device=dev)[None, :]).to(torch.int32)
+        oidx = db.out_index.to(torch.int32)
+        scratch = forward_indexed(b.d, b.n, b.stride, db.factors, fidx, db.inputs, db.outputs, oidx, stream=st)
+        ms = _timed(lambda: forward_indexed(b.d, b.n, b.stride, db.factors, fidx, db.inputs, db.outputs, oidx,
+                                            scratch=scratch, stream=st), st, reps)
+        emit(f"{cname}_fwd_f64_indexed", b, ms, 8, 8, launches=2)
         ref = reference_gpu_ms(db, reps=3)
         if ref is not None:
             emit(f"{cname}_reference_gpu_kernel_f64", b, ref, 8, 8,

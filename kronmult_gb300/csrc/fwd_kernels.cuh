@@ -100,6 +100,30 @@ template <typename T, int NN> __device__ __forceinline__ void load_fibre(const T
 template <typename T> __device__ __forceinline__ T fma_t(T a, T b, T c) { return fma(a, b, c); }
 template <> __device__ __forceinline__ float fma_t<float>(float a, float b, float c) { return fmaf(a, b, c); }
 
+// Factors too large to keep in registers (NN*NN*sizeof(T) > 128 bytes).
+template <typename T, int NN> struct FactorInSmem {
+    static constexpr bool value = NN * NN * sizeof(T) > 128;
+};
+
+// y[r] = sum_k M(r, k) * x[k] for one fibre, M col-major NN x NN in shared memory.
+// Column k is fetched with the widest aligned vector load (the layout keeps every
+// factor 16-byte aligned and a column's offset a multiple of the fibre load width)
+// and feeds all NN rows, so one broadcast load serves up to 16/sizeof(T) x NN FMAs
+// instead of one.  Each y[r] is still the k-ascending FMA chain from 0.
+template <typename T, int NN>
+__device__ __forceinline__ void mode_fibre_smem(const T *M, const T (&xv)[NN], T (&y)[NN])
+{
+#pragma unroll
+    for (int r = 0; r < NN; ++r) y[r] = T(0);
+#pragma unroll
+    for (int k = 0; k < NN; ++k) {
+        T col[NN];
+        load_fibre<T, NN>(M + k * NN, col);
+#pragma unroll
+        for (int r = 0; r < NN; ++r) y[r] = fma_t<T>(col[r], xv[k], y[r]);
+    }
+}
+
 // ---- asynchronous global->shared copies (cp.async, completion per thread) --
 
 template <int BYTES> __device__ __forceinline__ void cp_async(void *dst, const void *src)
@@ -210,7 +234,7 @@ __device__ __forceinline__ void team_forward(const T *const *mats, const T *cons
             const T *M = fac + i * NN * NN;
             // small factors are held in registers; larger ones are read from shared
             // memory, where every lane of a warp reads the same address (broadcast)
-            constexpr bool kRegM = NN * NN * sizeof(T) <= 128;
+            constexpr bool kRegM = !FactorInSmem<T, NN>::value;
             T m[kRegM ? NN * NN : 1];
             if constexpr (kRegM) {
 #pragma unroll
@@ -222,15 +246,16 @@ __device__ __forceinline__ void team_forward(const T *const *mats, const T *cons
                 if (c < F) {
                     T xv[NN];
                     load_fibre<T, NN>(buf + c * NN, xv);
+                    if constexpr (kRegM) {
 #pragma unroll
-                    for (int r = 0; r < NN; ++r) {
-                        T s = T(0);
+                        for (int r = 0; r < NN; ++r) {
+                            T s = T(0);
 #pragma unroll
-                        for (int k = 0; k < NN; ++k) {
-                            const T mv = kRegM ? m[kRegM ? r + k * NN : 0] : M[r + k * NN];
-                            s = fma_t<T>(mv, xv[k], s);
+                            for (int k = 0; k < NN; ++k) s = fma_t<T>(m[r + k * NN], xv[k], s);
+                            y[q][r] = s;
                         }
-                        y[q][r] = s;
+                    } else {
+                        mode_fibre_smem<T, NN>(M, xv, y[q]);
                     }
                 }
             }
@@ -532,12 +557,16 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) fwd_single_kernel
             if (c < F) {
                 T xv[NN];
                 load_fibre<T, NN>(buf + c * NN, xv);
+                if constexpr (FactorInSmem<T, NN>::value) {
+                    mode_fibre_smem<T, NN>(M, xv, y[q]);
+                } else {
 #pragma unroll
-                for (int r = 0; r < NN; ++r) {
-                    T s = T(0);
+                    for (int r = 0; r < NN; ++r) {
+                        T s = T(0);
 #pragma unroll
-                    for (int k = 0; k < NN; ++k) s = fma_t<T>(M[r + k * NN], xv[k], s);
-                    y[q][r] = s;
+                        for (int k = 0; k < NN; ++k) s = fma_t<T>(M[r + k * NN], xv[k], s);
+                        y[q][r] = s;
+                    }
                 }
             }
         }

@@ -130,7 +130,9 @@ int plan_forward(FwdPlan<T, TO> &pl, int d, int n, const T *const *mats, int str
         const int qcap = (n <= 4) ? 8 : 4;
         int ts = 8;
         if (tune && tune->team_size > 0) {
+            // a forced team size grows until every thread holds at most qcap fibres
             ts = tune->team_size;
+            while (ts < 512 && (F + ts - 1) / ts > qcap) ts *= 2;
         } else {
             // smallest team that leaves every thread at most ~2-4 fibres
             const int qtarget = (n <= 4) ? 4 : 2;
