@@ -39,7 +39,33 @@ template <typename T, typename TO> struct FwdArgs {
 
 // copy N values of an input vector into shared memory, 16-byte vectors when the
 // source is 16-byte aligned and N*sizeof(T) is a multiple of 16
-template <typename T>
+// ---- swizzled vector layout ------------------------------------------------
+// Fibres of 32 bytes (two 16-byte chunks) read by consecutive lanes would put two
+// lanes of a quarter-warp on the same banks.  FP32 vectors with n = 8 are staged
+// with 16-byte chunk ch stored at chunk ch ^ ((ch >> 3) & 7): the chunks one
+// quarter-warp reads then land on distinct banks, and each aligned group of 8
+// chunks (one 128-byte row) is only permuted within itself, so stores of
+// consecutive elements stay conflict-free.  (FP64 kernels are bound by the FP64
+// pipe, not by shared memory, and keep the plain layout and its lower register
+// count.)
+template <typename T, int NN> struct VecSwizzle {
+    static constexpr bool on = sizeof(T) == 4 && NN * sizeof(T) == 32;
+};
+
+__device__ __forceinline__ int swz_chunk(int ch) { return ch ^ ((ch >> 3) & 7); }
+
+// shared-memory position of vector element e
+template <typename T, bool SWZ> __device__ __forceinline__ int vec_pos(int e)
+{
+    if constexpr (SWZ) {
+        constexpr int per = 16 / (int)sizeof(T);
+        return swz_chunk(e / per) * per + (e & (per - 1));
+    } else {
+        return e;
+    }
+}
+
+template <typename T, bool SWZ = false>
 __device__ __forceinline__ void stage_vector(T *dst, const T *src, int N, const Team &tm)
 {
     const size_t bytes = (size_t)N * sizeof(T);
@@ -47,9 +73,9 @@ __device__ __forceinline__ void stage_vector(T *dst, const T *src, int N, const 
         const int nv = (int)(bytes >> 4);
         int4 *d4 = reinterpret_cast<int4 *>(dst);
         const int4 *s4 = reinterpret_cast<const int4 *>(src);
-        for (int v = tm.rank; v < nv; v += tm.size) d4[v] = __ldcs(s4 + v);
+        for (int v = tm.rank; v < nv; v += tm.size) d4[SWZ ? swz_chunk(v) : v] = __ldcs(s4 + v);
     } else {
-        for (int v = tm.rank; v < N; v += tm.size) dst[v] = __ldcs(src + v);
+        for (int v = tm.rank; v < N; v += tm.size) dst[vec_pos<T, SWZ>(v)] = __ldcs(src + v);
     }
 }
 
@@ -124,6 +150,98 @@ __device__ __forceinline__ void mode_fibre_smem(const T *M, const T (&xv)[NN], T
     }
 }
 
+// The same for two fibres at once: each column load feeds 2 x NN FMAs.
+template <typename T, int NN>
+__device__ __forceinline__ void mode_fibre2_smem(const T *M, const T (&x0)[NN], const T (&x1)[NN], T (&y0)[NN],
+                                                 T (&y1)[NN])
+{
+#pragma unroll
+    for (int r = 0; r < NN; ++r) {
+        y0[r] = T(0);
+        y1[r] = T(0);
+    }
+#pragma unroll
+    for (int k = 0; k < NN; ++k) {
+        T col[NN];
+        load_fibre<T, NN>(M + k * NN, col);
+#pragma unroll
+        for (int r = 0; r < NN; ++r) {
+            y0[r] = fma_t<T>(col[r], x0[k], y0[r]);
+            y1[r] = fma_t<T>(col[r], x1[k], y1[r]);
+        }
+    }
+}
+
+// fibre c (NN values from element c*NN) of a staged vector, swizzled or not
+template <typename T, int NN, bool SWZ>
+__device__ __forceinline__ void load_fibre_v(const T *buf, int c, T (&x)[NN])
+{
+    if constexpr (SWZ) {
+        constexpr int P = NN * (int)sizeof(T) / 16;
+        const int4 *b4 = reinterpret_cast<const int4 *>(buf);
+#pragma unroll
+        for (int j = 0; j < P; ++j) {
+            const int4 t = b4[swz_chunk(c * P + j)];
+            *reinterpret_cast<int4 *>(&x[j * 16 / (int)sizeof(T)]) = t;
+        }
+    } else {
+        load_fibre<T, NN>(buf + c * NN, x);
+    }
+}
+
+// One mode product of a team over its fibres c = rank + q*size < F (q < QMAX):
+// y[q] = M . fibre c.  Factors held in registers (m) are used directly; factors in
+// shared memory are read a column at a time, shared by pairs of fibres.
+template <typename T, int NN, int QMAX, bool SWZ, bool REGM>
+__device__ __forceinline__ void mode_team(const T *buf, const T *M, const T *m, int F, const Team &tm,
+                                          T (&y)[QMAX][NN])
+{
+    if constexpr (REGM) {
+#pragma unroll
+        for (int q = 0; q < QMAX; ++q) {
+            const int c = tm.rank + q * tm.size;
+            if (c < F) {
+                T xv[NN];
+                load_fibre_v<T, NN, SWZ>(buf, c, xv);
+#pragma unroll
+                for (int r = 0; r < NN; ++r) {
+                    T s = T(0);
+#pragma unroll
+                    for (int k = 0; k < NN; ++k) s = fma_t<T>(m[r + k * NN], xv[k], s);
+                    y[q][r] = s;
+                }
+            }
+        }
+    } else {
+        // highest rank in this thread's warp (teams of fewer than 32 threads share a
+        // warp with other teams of the same size), so that the pair / single choice
+        // below is uniform across the warp
+        const int last = tm.size < 32 ? tm.size - 1 : (tm.rank | 31);
+#pragma unroll
+        for (int q = 0; q < QMAX; q += 2) {
+            const int c0 = tm.rank + q * tm.size;
+            if constexpr (QMAX >= 2) {
+                if (last + (q + 1) * tm.size < F) {
+                    T x0[NN], x1[NN];
+                    load_fibre_v<T, NN, SWZ>(buf, c0, x0);
+                    load_fibre_v<T, NN, SWZ>(buf, c0 + tm.size, x1);
+                    mode_fibre2_smem<T, NN>(M, x0, x1, y[q], y[q + 1]);
+                    continue;
+                }
+            }
+#pragma unroll
+            for (int h = 0; h < (QMAX >= 2 ? 2 : 1); ++h) {
+                const int c = c0 + h * tm.size;
+                if (c < F) {
+                    T x0[NN];
+                    load_fibre_v<T, NN, SWZ>(buf, c, x0);
+                    mode_fibre_smem<T, NN>(M, x0, y[q + h]);
+                }
+            }
+        }
+    }
+}
+
 // ---- asynchronous global->shared copies (cp.async, completion per thread) --
 
 template <int BYTES> __device__ __forceinline__ void cp_async(void *dst, const void *src)
@@ -140,7 +258,7 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 
 // issue the copies of one entry's input vector and factors into a staging slot
 // (same layouts as stage_vector / stage_factors); completes with cp_async_wait_all
-template <typename T, int NN>
+template <typename T, int NN, bool SWZ = false>
 __device__ __forceinline__ void stage_async(T *dst, T *fac, const T *src, const T *const *mats, int N, int d,
                                             int stride, const Team &tm)
 {
@@ -148,9 +266,10 @@ __device__ __forceinline__ void stage_async(T *dst, T *fac, const T *src, const 
     if (((reinterpret_cast<uintptr_t>(src) & 15u) == 0) && ((bytes & 15u) == 0)) {
         const int nv = (int)(bytes >> 4);
         for (int v = tm.rank; v < nv; v += tm.size)
-            cp_async<16>(reinterpret_cast<int4 *>(dst) + v, reinterpret_cast<const int4 *>(src) + v);
+            cp_async<16>(reinterpret_cast<int4 *>(dst) + (SWZ ? swz_chunk(v) : v),
+                         reinterpret_cast<const int4 *>(src) + v);
     } else {
-        for (int v = tm.rank; v < N; v += tm.size) cp_async<(int)sizeof(T)>(dst + v, src + v);
+        for (int v = tm.rank; v < N; v += tm.size) cp_async<(int)sizeof(T)>(dst + vec_pos<T, SWZ>(v), src + v);
     }
     constexpr int NN2 = NN * NN;
     for (int idx = tm.rank; idx < d * NN2; idx += tm.size) {
@@ -207,10 +326,11 @@ __device__ __forceinline__ void team_forward(const T *const *mats, const T *cons
         }
     };
 
+    constexpr bool kSwz = VecSwizzle<T, NN>::on;
     if constexpr (PF) {
         if (e_begin < e_end) {
             const long long e0 = perm ? perm[e_begin] : e_begin;
-            stage_async<T, NN>(buf, fac, in[e0], mats + e0 * d, N, d, stride, tm);
+            stage_async<T, NN, kSwz>(buf, fac, in[e0], mats + e0 * d, N, d, stride, tm);
         }
     }
     for (long long ei = e_begin; ei < e_end; ++ei) {
@@ -221,10 +341,10 @@ __device__ __forceinline__ void team_forward(const T *const *mats, const T *cons
             tm.sync();  // slot of entry e complete for the whole team
             if (ei + 1 < e_end) {
                 const long long en = perm ? perm[ei + 1] : ei + 1;
-                stage_async<T, NN>(buf2, fac2, in[en], mats + en * d, N, d, stride, tm);
+                stage_async<T, NN, kSwz>(buf2, fac2, in[en], mats + en * d, N, d, stride, tm);
             }
         } else {
-            stage_vector(buf, in[e], N, tm);
+            stage_vector<T, kSwz>(buf, in[e], N, tm);
             stage_factors<T, NN>(fac, mats + e * d, d, stride, tm);
             tm.sync();
         }
@@ -240,25 +360,7 @@ __device__ __forceinline__ void team_forward(const T *const *mats, const T *cons
 #pragma unroll
                 for (int j = 0; j < NN * NN; ++j) m[j] = M[j];
             }
-#pragma unroll
-            for (int q = 0; q < QMAX; ++q) {
-                const int c = tm.rank + q * tm.size;
-                if (c < F) {
-                    T xv[NN];
-                    load_fibre<T, NN>(buf + c * NN, xv);
-                    if constexpr (kRegM) {
-#pragma unroll
-                        for (int r = 0; r < NN; ++r) {
-                            T s = T(0);
-#pragma unroll
-                            for (int k = 0; k < NN; ++k) s = fma_t<T>(m[r + k * NN], xv[k], s);
-                            y[q][r] = s;
-                        }
-                    } else {
-                        mode_fibre_smem<T, NN>(M, xv, y[q]);
-                    }
-                }
-            }
+            mode_team<T, NN, QMAX, kSwz, kRegM>(buf, M, m, F, tm, y);
             tm.sync();  // every read of buf (and fac) for this mode is done
             if (i > 0) {
 #pragma unroll
@@ -266,7 +368,7 @@ __device__ __forceinline__ void team_forward(const T *const *mats, const T *cons
                     const int c = tm.rank + q * tm.size;
                     if (c < F) {
 #pragma unroll
-                        for (int r = 0; r < NN; ++r) buf[c + r * F] = y[q][r];
+                        for (int r = 0; r < NN; ++r) buf[vec_pos<T, kSwz>(c + r * F)] = y[q][r];
                     }
                 }
                 tm.sync();
@@ -545,31 +647,16 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) fwd_single_kernel
     const long long e = (long long)blockIdx.x * a.teams_per_cta + tm.id;
     if (e >= a.nb) return;
     const int F = a.N / NN;
-    stage_vector(buf, a.in[e], a.N, tm);
+    constexpr bool kSwz = VecSwizzle<T, NN>::on;
+    stage_vector<T, kSwz>(buf, a.in[e], a.N, tm);
     stage_factors<T, NN>(fac, a.mats + e * a.d, a.d, a.stride, tm);
     tm.sync();
     T y[QMAX][NN];
     for (int i = a.d - 1; i >= 0; --i) {
         const T *M = fac + i * NN * NN;
-#pragma unroll
-        for (int q = 0; q < QMAX; ++q) {
-            const int c = tm.rank + q * tm.size;
-            if (c < F) {
-                T xv[NN];
-                load_fibre<T, NN>(buf + c * NN, xv);
-                if constexpr (FactorInSmem<T, NN>::value) {
-                    mode_fibre_smem<T, NN>(M, xv, y[q]);
-                } else {
-#pragma unroll
-                    for (int r = 0; r < NN; ++r) {
-                        T s = T(0);
-#pragma unroll
-                        for (int k = 0; k < NN; ++k) s = fma_t<T>(M[r + k * NN], xv[k], s);
-                        y[q][r] = s;
-                    }
-                }
-            }
-        }
+        // small factors are read from shared memory per use (the compiler keeps them
+        // in registers where it can); large ones a column at a time
+        mode_team<T, NN, QMAX, kSwz, !FactorInSmem<T, NN>::value>(buf, M, M, F, tm, y);
         if (i > 0) {
             tm.sync();
 #pragma unroll
@@ -577,7 +664,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) fwd_single_kernel
                 const int c = tm.rank + q * tm.size;
                 if (c < F) {
 #pragma unroll
-                    for (int r = 0; r < NN; ++r) buf[c + r * F] = y[q][r];
+                    for (int r = 0; r < NN; ++r) buf[vec_pos<T, kSwz>(c + r * F)] = y[q][r];
                 }
             }
             tm.sync();
