@@ -485,9 +485,19 @@ def suite(args):
         torch.cuda.synchronize()
         res[dt] = (ms, db.outputs.double().cpu().numpy(), gin.double().cpu().numpy(), gfa.double().cpu().numpy())
     (m64, y64, gi64, ga64), (m32, y32, gi32, ga32) = res[torch.float64], res[torch.float32]
-    emit("c5_fwd_adj_f64_plain", b, m64, 8, 8, {"adjoint_flops_note": "gflops counts forward flops only"},
-         launches=2)
-    emit("c5_fwd_adj_f32_graph", b, m32, 4, 4, {
+
+    class _FwdAdj:  # forward + grad_input + grad_A contractions: 3 x 2dnN per entry
+        def flops(self_):
+            return 3.0 * b.flops()
+
+        def bytes(self_, i, o):
+            # x and g read, grad_input written, factors read and grad_A written, outputs once
+            return b.bytes(i, o) + i * b.N * b.nb * 2 + 2.0 * i * b.n * b.n * b.d * b.n_sets
+
+    fm = {"flops_model": "3 x 2dnN per entry (forward, grad_input, grad_A contractions; "
+                         "the partial products grad_A needs are not counted)"}
+    emit("c5_fwd_adj_f64_plain", _FwdAdj(), m64, 8, 8, fm, launches=2)
+    emit("c5_fwd_adj_f32_graph", _FwdAdj(), m32, 4, 4, {**fm,
         "speedup_vs_plain_fp64": m64 / m32,
         "rel_l2_vs_fp64": {"output": O.rel_l2(y32, y64), "grad_input": O.rel_l2(gi32, gi64),
                            "grad_factors": O.rel_l2(ga32, ga64)}}, launches=2)

@@ -85,7 +85,82 @@ template <typename T, typename TO> struct FwdPlan {
     int use_smem = 0;        // generic kernel: shared-memory ping-pong
     dim3 grid, block;
     size_t smem = 0;
+    const void *fn2 = nullptr;  // second launch (pass 2 of the two-pass path), same arguments
+    dim3 grid2, block2;
+    size_t smem2 = 0;
 };
+
+// Fibres per thread the two-pass path's pass-1 kernel is instantiated for, by n.
+inline int split_qmax(int n) { return n <= 3 ? 8 : (n <= 7 ? 4 : 2); }
+
+// Two-pass plan for vectors beyond shared memory (split_pass1/2_kernel): the
+// largest fast part n^d1 one 256-thread team sweeps in registers, then tiles of
+// L fast positions for pass 2.  Returns false where no split fits.
+template <typename T, typename TO>
+bool plan_split(FwdPlan<T, TO> &pl, const DeviceInfo &di)
+{
+    FwdArgs<T, TO> &a = pl.args;
+    const int n = a.n, d = a.d;
+    // FP64 stays on the one-vector global sweep: it is bound by the FP64 pipe, which
+    // the two passes do not relieve (measured slower on n = 8, d = 6)
+    if (sizeof(T) == 8 || n < 2 || n > 8 || d < 2 || !a.ws) return false;
+    const int qm = split_qmax(n);
+    constexpr int kAlign = 16 / (int)sizeof(T);
+    for (int d1 = d - 1; d1 >= 1; --d1) {
+        const long long C = pow_ll(n, d1), F1 = C / n, R = pow_ll(n, d - d1);
+        if (F1 > 256LL * qm || R > 4096) continue;
+        int ts = 8;
+        while (ts < 256 && (long long)ts * qm < F1) ts *= 2;
+        const int vpad = round_up((int)C, kAlign), fpad = round_up(d1 * n * n, kAlign);
+        const int teams = 256 / ts;
+        const size_t smem1 = (size_t)teams * (vpad + fpad) * sizeof(T);
+        auto f1 = split_pass1_lookup<T, TO>(n, qm);
+        auto f2 = split_pass2_lookup<T, TO>(n);
+        if (!f1 || !f2 || smem1 > (size_t)di.max_smem_optin) continue;
+        // pass-2 tile: rows of at least 128 bytes and at least 256 (fibre, position)
+        // tasks per mode, where two tiles fit in half the SM; else narrower (32 bytes
+        // at least)
+        const int fpad2 = round_up((d - d1) * n * n, kAlign);
+        int L = 128 / (int)sizeof(T);
+        while ((long long)L * (R / n) < 512 && L < 512) L *= 2;
+        while (L > 32 / (int)sizeof(T) &&
+               (4 * R * L + 2 * fpad2) * (long long)sizeof(T) > (long long)di.max_smem_optin / 2)
+            L /= 2;
+        const size_t smem2 = (size_t)(4 * R * L + 2 * fpad2) * sizeof(T);
+        if (smem2 > (size_t)di.max_smem_optin) return false;
+        const long long tiles = (C + L - 1) / L;
+        // pass 2 sums runs of up to 64 consecutive entries per CTA while leaving ~16
+        // CTAs per SM
+        long long ept2 = a.nb * tiles / (16LL * di.sms);
+        if (ept2 > 64) ept2 = 64;
+        if (ept2 < 1) ept2 = 1;
+        const long long grid1 = (a.nb * R + teams - 1) / teams, grid2 = (a.nb + ept2 - 1) / ept2 * tiles;
+        if (grid1 > INT_MAX || grid2 > INT_MAX) return false;
+        if (!ensure_smem_attr((const void *)f1, smem1) || !ensure_smem_attr((const void *)f2, smem2)) return false;
+        a.team_size = ts;
+        a.teams_per_cta = teams;
+        a.entries_per_team = (int)ept2;  // pass 2 only; pass 1 runs one chunk per team
+        a.team_elems = vpad + fpad;
+        a.vec_pad = vpad;
+        a.fac_pad = fpad;
+        a.prefetch = 0;
+        a.split_d1 = d1;
+        a.split_C = (int)C;
+        a.split_R = (int)R;
+        a.split_L = L;
+        pl.fn = (const void *)f1;
+        pl.smem_path = true;
+        pl.grid = dim3((unsigned)grid1);
+        pl.block = dim3((unsigned)(teams * ts));
+        pl.smem = smem1;
+        pl.fn2 = (const void *)f2;
+        pl.grid2 = dim3((unsigned)grid2);
+        pl.block2 = dim3(256);
+        pl.smem2 = smem2;
+        return true;
+    }
+    return false;
+}
 
 // Checks arguments and fills a plan.  Returns cudaSuccess, cudaErrorInvalidValue,
 // or cudaErrorNotSupported (vector too long for any path without a workspace).
@@ -99,6 +174,7 @@ int plan_forward(FwdPlan<T, TO> &pl, int d, int n, const T *const *mats, int str
     if (Nl > (long long)INT_MAX) return cudaErrorInvalidValue;
     pl.args = FwdArgs<T, TO>{};
     pl.fn = nullptr;
+    pl.fn2 = nullptr;
     kronmult_tuning cached{};
     if (!tune) {
         const int code = sizeof(T) == 8 ? KRONMULT_DTYPE_F64
@@ -297,7 +373,10 @@ int plan_forward(FwdPlan<T, TO> &pl, int d, int n, const T *const *mats, int str
         }
     }
 
-    // ---- large vectors through input/workspace in global memory (compile-time n)
+    // ---- large vectors: two passes through the workspace (input left intact)
+    if (plan_split<T, TO>(pl, di)) return cudaSuccess;
+
+    // ---- larger still: every mode through input/workspace in global memory
     if (n >= 2 && n <= 8 && d >= 1 && ws) {
         const size_t smem_s = ((size_t)round_up(n * n, 2) + 2 * (size_t)round_up(N, 2)) * sizeof(T);
         if (smem_s > (size_t)di.max_smem_optin) {
@@ -344,6 +423,10 @@ template <typename T, typename TO> int launch_plan(const FwdPlan<T, TO> &pl, cud
     if (pl.smem_path) {
         auto fn = reinterpret_cast<void (*)(const FwdArgs<T, TO>)>(const_cast<void *>(pl.fn));
         fn<<<pl.grid, pl.block, pl.smem, st>>>(pl.args);
+        if (pl.fn2) {
+            auto fn2 = reinterpret_cast<void (*)(const FwdArgs<T, TO>)>(const_cast<void *>(pl.fn2));
+            fn2<<<pl.grid2, pl.block2, pl.smem2, st>>>(pl.args);
+        }
     } else {
         auto fn = reinterpret_cast<void (*)(const FwdArgs<T, TO>, int)>(const_cast<void *>(pl.fn));
         fn<<<pl.grid, pl.block, pl.smem, st>>>(pl.args, pl.use_smem);

@@ -150,14 +150,51 @@ def test_aliased_inputs(cuda):
     assert O.rel_l2(db.outputs.cpu().numpy(), O.forward(b2)) <= TOL64
 
 
-def test_large_vector_global_path(cuda):
-    """n^d beyond shared memory goes through input/workspace in global memory."""
+def test_large_vector_two_pass(cuda):
+    """n^d beyond shared memory: two passes through the workspace; the input is only read."""
+    from kronmult_gb300 import DeviceBatch
+    from kronmult_gb300 import workloads as W
+
+    b = W.make_batch(5, 8, 8, 1, 2, seed=31)  # N = 32768: 128 KiB in FP32
+    ref = O.forward(b)
+    db = DeviceBatch.from_host(b, device=cuda, dtype=torch.float32, with_workspace=True)
+    x0 = db.inputs.clone()
+    db.forward(sync=True)
+    assert O.rel_l2(db.outputs.double().cpu().numpy(), ref) <= TOL32
+    assert torch.equal(db.inputs, x0)
+
+
+def test_large_vector_global_sweep_f64(cuda):
+    """FP64 vectors beyond shared memory: every mode through input/workspace."""
     from kronmult_gb300 import workloads as W
 
     b = W.make_batch(5, 8, 8, 1, 2, seed=31)  # N = 32768 doubles = 256 KiB
-    ref = O.forward(b)
     got, _ = run(b, cuda, ws=True)
-    assert O.rel_l2(got, ref) <= TOL64
+    assert O.rel_l2(got, O.forward(b)) <= TOL64
+
+
+@pytest.mark.parametrize("d,n,dtype", [(10, 3, torch.float32), (7, 5, torch.float32), (8, 4, torch.float32),
+                                       (16, 2, torch.float32), (5, 7, torch.float32), (7, 6, torch.float32),
+                                       (10, 3, torch.float64), (8, 4, torch.float64)])
+def test_large_vector_two_pass_shapes(cuda, d, n, dtype):
+    """FP32 two-pass path with partial pass-2 tiles (n = 3, 5, 7) and every n; FP64
+    shapes of the same sizes take the global sweep."""
+    from kronmult_gb300 import workloads as W
+
+    b = W.make_batch(d, n, n + 1, 3, 2, seed=700 + 10 * d + n)
+    got, _ = run(b, cuda, dtype=dtype, ws=True)
+    tol = TOL64 if dtype == torch.float64 else TOL32
+    assert O.rel_l2(got, O.forward(b)) <= tol
+
+
+def test_large_vector_global_fallback(cuda):
+    """Beyond the two-pass limits (n = 2, d = 25: 2^12 slow positions would remain for
+    pass 2) every mode goes through input/workspace in global memory."""
+    from kronmult_gb300 import workloads as W
+
+    b = W.make_batch(25, 2, 2, 1, 1, seed=32)  # N = 33554432
+    got, _ = run(b, cuda, dtype=torch.float32, ws=True)
+    assert O.rel_l2(got, O.forward(b)) <= TOL32
 
 
 def test_reference_signature_mirror(cuda):

@@ -47,6 +47,23 @@ def test_bitwise_per_entry_f64(cuda, d, n, stride):
     assert torch.equal(db.outputs, want)
 
 
+@pytest.mark.parametrize("d,n,stride,dtype", [(5, 8, 8, torch.float64), (10, 3, 4, torch.float64),
+                                              (5, 8, 8, torch.float32), (6, 8, 67, torch.float64)])
+def test_bitwise_per_entry_large(cuda, d, n, stride, dtype):
+    """Vectors beyond shared memory (two passes through the workspace) against the
+    reference kernel's one-vector sweep: identical bits per entry."""
+    needs_ref()
+    from kronmult_gb300 import DeviceBatch
+    from kronmult_gb300 import workloads as W
+
+    nb = 3 if n ** d > 100000 else 12
+    b = W.make_batch(d, n, stride, nb, 1, seed=660 + d * 10 + n)
+    db = DeviceBatch.from_host(b, device=cuda, dtype=dtype, with_workspace=True)
+    want = reference_run(db, "f64" if dtype == torch.float64 else "f32")
+    db.forward(sync=True)
+    assert torch.equal(db.outputs, want)
+
+
 def test_bitwise_per_entry_f32(cuda):
     needs_ref()
     from kronmult_gb300 import DeviceBatch
