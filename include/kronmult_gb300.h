@@ -21,10 +21,12 @@
  *    The _async entry points only enqueue work: they neither allocate nor
  *    synchronise, so they can be captured in a CUDA graph.
  *  - Inputs are not modified when N*sizeof(T) fits in shared memory (every
- *    vector length the fast paths cover); larger vectors are processed through
- *    `input` and `workspace` in global memory, which are then clobbered as in the
- *    reference (kronmult_gpu/kronmult.cu:119-121).  `workspace_batched` may be
- *    NULL when no entry needs the global path.
+ *    vector length the fast paths cover).  Larger vectors need `workspace`: FP32
+ *    ones go through it in two passes and leave `input` intact; FP64 ones (and
+ *    FP32 ones beyond the two-pass limits) are processed through `input` and
+ *    `workspace` in global memory, which are then clobbered as in the reference
+ *    (kronmult_gpu/kronmult.cu:119-121).  `workspace_batched` may be NULL when no
+ *    entry needs a global-memory path.
  *  - 0 <= n, 0 <= d, n^d <= 2^31-1, matrix_stride >= max(n, 1), nb_batch >= 0.
  */
 #ifndef KRONMULT_GB300_H
