@@ -38,6 +38,7 @@ template <typename T, typename TO> struct FwdArgs {
     int split_C;           // n^split_d1: chunk of contiguous values pass 1 sweeps
     int split_R;           // n^(d-split_d1): values sharing a fast position (stride split_C)
     int split_L;           // fast positions per pass-2 tile
+    int split_ept1;        // chunks each pass-1 team sweeps (the next one copied while computing)
 };
 
 // ---- helpers ---------------------------------------------------------------
@@ -834,8 +835,10 @@ __global__ void __launch_bounds__(512) fwd_global_kernel(const FwdArgs<T, TO> a)
 // that traffic is the bound; FP64 stays on the global sweep, bound by its FP64
 // pipe.
 
-// Pass 1: one team per (entry, chunk), the register in-place sweep of the
-// shared-memory kernels over d1 modes; results stored to the workspace.
+// Pass 1: each team sweeps a range of (entry, chunk) units with the register
+// in-place sweep of the shared-memory kernels over d1 modes, two staging slots
+// (the next unit's chunk and factors copied by cp.async while the current one is
+// computed); results are stored to the workspace.
 template <typename T, typename TO, int NN, int QMAX>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) split_pass1_kernel(const FwdArgs<T, TO> a)
 {
@@ -843,41 +846,59 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) split_pass1_kerne
     const Team tm(a.team_size);
     T *buf = reinterpret_cast<T *>(smem_raw) + (size_t)tm.id * a.team_elems;
     T *fac = buf + a.vec_pad;
-    const long long w = (long long)blockIdx.x * a.teams_per_cta + tm.id;
-    if (w >= a.nb * (long long)a.split_R) return;
-    const long long e = w / a.split_R;
-    const size_t off = (size_t)(w - e * a.split_R) * (size_t)a.split_C;
-    const int C = a.split_C, F = C / NN, d1 = a.split_d1;
+    T *buf2 = fac + a.fac_pad;
+    T *fac2 = buf2 + a.vec_pad;
+    const long long units = a.nb * (long long)a.split_R;
+    const long long w_begin = ((long long)blockIdx.x * a.teams_per_cta + tm.id) * a.split_ept1;
+    if (w_begin >= units) return;
+    const long long w_end = min(w_begin + (long long)a.split_ept1, units);
+    const int C = a.split_C, F = C / NN, d1 = a.split_d1, d2 = a.d - d1;
     constexpr bool kSwz = VecSwizzle<T, NN>::on;
-    stage_vector<T, kSwz>(buf, a.in[e] + off, C, tm);
-    stage_factors<T, NN>(fac, a.mats + e * a.d + (a.d - d1), d1, a.stride, tm);
-    tm.sync();
-    T y[QMAX][NN];
-    for (int i = d1 - 1; i >= 0; --i) {
-        const T *M = fac + i * NN * NN;
-        mode_team<T, NN, QMAX, kSwz, !FactorInSmem<T, NN>::value>(buf, M, M, F, tm, y);
-        if (i > 0) {
-            tm.sync();
+    auto stage = [&](long long w, T *b, T *f) {
+        const long long e = w / a.split_R;
+        const size_t off = (size_t)(w - e * a.split_R) * (size_t)C;
+        stage_async<T, NN, kSwz>(b, f, a.in[e] + off, a.mats + e * a.d + d2, C, d1, a.stride, tm);
+    };
+    stage(w_begin, buf, fac);
+    for (long long w = w_begin; w < w_end; ++w) {
+        cp_async_wait_all();
+        tm.sync();  // chunk w staged for the whole team; every read of the other slot done
+        if (w + 1 < w_end) stage(w + 1, buf2, fac2);
+        T y[QMAX][NN];
+        for (int i = d1 - 1; i >= 0; --i) {
+            const T *M = fac + i * NN * NN;
+            mode_team<T, NN, QMAX, kSwz, !FactorInSmem<T, NN>::value>(buf, M, M, F, tm, y);
+            if (i > 0) {
+                tm.sync();
 #pragma unroll
-            for (int q = 0; q < QMAX; ++q) {
-                const int c = tm.rank + q * tm.size;
-                if (c < F) {
+                for (int q = 0; q < QMAX; ++q) {
+                    const int c = tm.rank + q * tm.size;
+                    if (c < F) {
 #pragma unroll
-                    for (int r = 0; r < NN; ++r) buf[vec_pos<T, kSwz>(c + r * F)] = y[q][r];
+                        for (int r = 0; r < NN; ++r) buf[vec_pos<T, kSwz>(c + r * F)] = y[q][r];
+                    }
                 }
+                tm.sync();
             }
-            tm.sync();
         }
-    }
-    T *dst = a.ws[e] + off;
+        const long long e = w / a.split_R;
+        T *dst = a.ws[e] + (size_t)(w - e * a.split_R) * (size_t)C;
 #pragma unroll
-    for (int q = 0; q < QMAX; ++q) {
-        const int c = tm.rank + q * tm.size;
-        if (c < F) {
+        for (int q = 0; q < QMAX; ++q) {
+            const int c = tm.rank + q * tm.size;
+            if (c < F) {
 #pragma unroll
-            for (int r = 0; r < NN; ++r) dst[c + r * F] = y[q][r];
+                for (int r = 0; r < NN; ++r) dst[c + r * F] = y[q][r];
+            }
         }
+        T *t = buf;
+        buf = buf2;
+        buf2 = t;
+        t = fac;
+        fac = fac2;
+        fac2 = t;
     }
+    cp_async_wait_all();
 }
 
 // Pass 2: one CTA per (tile of L fast positions, range of entries).  The tile is

@@ -113,7 +113,7 @@ bool plan_split(FwdPlan<T, TO> &pl, const DeviceInfo &di)
         while (ts < 256 && (long long)ts * qm < F1) ts *= 2;
         const int vpad = round_up((int)C, kAlign), fpad = round_up(d1 * n * n, kAlign);
         const int teams = 256 / ts;
-        const size_t smem1 = (size_t)teams * (vpad + fpad) * sizeof(T);
+        const size_t smem1 = (size_t)teams * 2 * (vpad + fpad) * sizeof(T);  // two staging slots
         auto f1 = split_pass1_lookup<T, TO>(n, qm);
         auto f2 = split_pass2_lookup<T, TO>(n);
         if (!f1 || !f2 || smem1 > (size_t)di.max_smem_optin) continue;
@@ -134,16 +134,22 @@ bool plan_split(FwdPlan<T, TO> &pl, const DeviceInfo &di)
         long long ept2 = a.nb * tiles / (16LL * di.sms);
         if (ept2 > 64) ept2 = 64;
         if (ept2 < 1) ept2 = 1;
-        const long long grid1 = (a.nb * R + teams - 1) / teams, grid2 = (a.nb + ept2 - 1) / ept2 * tiles;
+        // pass 1: up to 8 chunks per team while leaving ~8 CTAs per SM
+        long long ept1 = a.nb * R / ((long long)teams * di.sms * 8);
+        if (ept1 > 8) ept1 = 8;
+        if (ept1 < 1) ept1 = 1;
+        const long long per_cta1 = (long long)teams * ept1;
+        const long long grid1 = (a.nb * R + per_cta1 - 1) / per_cta1, grid2 = (a.nb + ept2 - 1) / ept2 * tiles;
         if (grid1 > INT_MAX || grid2 > INT_MAX) return false;
         if (!ensure_smem_attr((const void *)f1, smem1) || !ensure_smem_attr((const void *)f2, smem2)) return false;
         a.team_size = ts;
         a.teams_per_cta = teams;
         a.entries_per_team = (int)ept2;  // pass 2 only; pass 1 runs one chunk per team
-        a.team_elems = vpad + fpad;
+        a.team_elems = 2 * (vpad + fpad);
         a.vec_pad = vpad;
         a.fac_pad = fpad;
-        a.prefetch = 0;
+        a.prefetch = 1;
+        a.split_ept1 = (int)ept1;
         a.split_d1 = d1;
         a.split_C = (int)C;
         a.split_R = (int)R;
