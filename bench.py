@@ -13,8 +13,10 @@ value       GFLOP/s (algorithmic 2*d*n*N flops per entry) over K device-timed st
             flush is needed between steps)
 e2e         the same metric through the public API with host (pinned) buffers:
             each step copies the inputs and factors in and the outputs back
-            (api.forward_from_host: 8 pieces, copies overlapping the forward),
-            host wall clock per step including the final synchronisation
+            (api.forward_from_host: 12 pieces, copies overlapping the forward),
+            host wall clock per step including the final synchronisation; beside
+            it, e2e.mapped_inputs: the kernels read inputs and factors straight
+            from pinned host memory (api.forward_from_host_mapped)
 roofline    the forward kernel against the roof that binds it; for FP64 that is the
             FP64 FMA pipe, measured live (HBM fraction reported beside it)
 cpu_baseline  the C oracle (a restatement of the reference's kronmult_omp) on the
@@ -568,27 +570,38 @@ def main():
     h2d = h_in.numel() * esize + h_fac.numel() * esize
     d2h = h_out.numel() * esize
 
-    from kronmult_gb300.api import forward_from_host
+    from kronmult_gb300.api import forward_from_host, forward_from_host_mapped
 
     pipe_streams = (torch.cuda.Stream(dev), torch.cuda.Stream(dev), torch.cuda.Stream(dev))
 
     def e2e_step():
-        # copies in, forward, copy out: pipelined in 8 pieces over three streams
-        forward_from_host(db, h_in, h_fac, h_out, chunks=8, streams=pipe_streams)
+        # copies in, forward, copy out: pipelined in 12 pieces over three streams
+        forward_from_host(db, h_in, h_fac, h_out, chunks=12, streams=pipe_streams)
 
-    e2e_step()
-    torch.cuda.synchronize()
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.e2e_steps):
-        e2e_step()
-        torch.cuda.synchronize()  # the host result is complete at the end of every step
-    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.e2e_steps
-    if world > 1:
-        t = torch.tensor([e2e_ms], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = t.item()
+    def e2e_mapped_step():
+        # kernels read inputs and factors from pinned host memory; outputs copied back in 2 pieces
+        forward_from_host_mapped(db, h_in, h_fac, h_out, chunks=2, streams=pipe_streams)
+
+    def time_host_steps(step):
+        step()
+        torch.cuda.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            step()
+            torch.cuda.synchronize()  # the host result is complete at the end of every step
+        ms = (time.perf_counter() - t0) * 1e3 / args.e2e_steps
+        if world > 1:
+            t = torch.tensor([ms], device=dev, dtype=torch.float64)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = t.item()
+        return ms
+
+    e2e_ms = time_host_steps(e2e_step)
     e2e_value = flops_step * world / (e2e_ms / 1e3) / 1e9
+    e2e_mapped_ms = None
+    if tdt == torch.float64 and h_in.shape == db.inputs.shape and h_fac.shape == db.factors.shape:
+        e2e_mapped_ms = time_host_steps(e2e_mapped_step)
 
     # ---- live roofline denominators
     fp64_peak = None
@@ -657,7 +670,12 @@ def main():
             "cpu_baseline": cpu,
             "reference_gpu_kernel": ref_gpu_line,
             "e2e": {"value": e2e_value, "unit": "GFLOP/s", "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms},
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
+                    "path": "api.forward_from_host: staging copies from pinned host memory, 12 pieces",
+                    "mapped_inputs": None if e2e_mapped_ms is None else {
+                        "ms_per_step": e2e_mapped_ms, "value": flops_step * world / (e2e_mapped_ms / 1e3) / 1e9,
+                        "path": "api.forward_from_host_mapped: kernels read inputs and factors from pinned "
+                                "host memory over the CPU-GPU link, outputs copied back"}},
             "gpu_launches": args.steps,
             "clocks": clk,
         }

@@ -240,6 +240,14 @@ int kronmult_indexed_f32_async(int matrix_count, int matrix_size, int matrix_str
                                long long output_pitch, const int *output_index, int nb_batch, void *scratch,
                                long long scratch_bytes, void *stream);
 
+/*
+ * Device address of page-locked host memory (cudaHostGetDevicePointer), for pointer
+ * arrays whose inputs the kernels read straight from host memory over the
+ * CPU-GPU link instead of copying them first (no reference counterpart).  Fails
+ * (non-zero status, *device = NULL) for memory that is not page-locked and mapped.
+ */
+int kronmult_host_device_pointer(const void *host, void **device);
+
 /* Integer power as in the reference's pow_int (kronmult_gpu/kronmult.cuh:10), in 64 bits. */
 long long kronmult_pow_int(int number, int power);
 

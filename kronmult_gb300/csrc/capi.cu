@@ -292,4 +292,11 @@ const char *kronmult_error_string(int status) { return cudaGetErrorString((cudaE
 
 int kronmult_abi_version(void) { return KRONMULT_GB300_VERSION; }
 
+int kronmult_host_device_pointer(const void *host, void **device)
+{
+    if (!host || !device) return cudaErrorInvalidValue;
+    *device = nullptr;
+    return (int)cudaHostGetDevicePointer(device, const_cast<void *>(host), 0);
+}
+
 }  // extern "C"

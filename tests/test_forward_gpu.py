@@ -298,3 +298,25 @@ def test_large_published_shape(cuda, dtype):
     got, _ = run(b, cuda, dtype=dtype, ws=True)
     tol = TOL64 if dtype == torch.float64 else TOL32
     assert O.rel_l2(got, O.forward(b)) <= tol
+
+
+@pytest.mark.parametrize("chunks", [1, 2, 5])
+def test_forward_from_host_pipelines(cuda, chunks):
+    """The end-to-end host pipelines (staging copies, and kernels reading pinned host
+    memory directly) against the device-resident forward and the oracle."""
+    from kronmult_gb300 import DeviceBatch
+    from kronmult_gb300 import workloads as W
+    from kronmult_gb300.api import forward_from_host, forward_from_host_mapped
+
+    b = W.config2(scale=24 / 4096)
+    ref = O.forward(b)
+    db = DeviceBatch.from_host(b, device=cuda)
+    h_in = torch.from_numpy(b.inputs).pin_memory()
+    h_fac = torch.from_numpy(b.factors).pin_memory()
+    for fn in (forward_from_host, forward_from_host_mapped):
+        db.outputs.zero_()
+        h_out = torch.full(db.outputs.shape, float("nan"), dtype=torch.float64).pin_memory()
+        torch.cuda.synchronize()
+        fn(db, h_in, h_fac, h_out, chunks=chunks)
+        torch.cuda.synchronize()
+        assert O.rel_l2(h_out.numpy(), ref) <= TOL64
