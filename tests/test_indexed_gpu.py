@@ -57,3 +57,31 @@ def test_indexed_rejects_small_scratch(cuda):
                                         8, None)
     assert rc == 1
     assert lib.kronmult_indexed_scratch_bytes(3, 10) == 10 * 5 * 8
+
+
+def test_indexed_graph_capture(cuda):
+    """The indexed forward (table expansion + forward) captured in a CUDA graph and
+    replayed twice adds the product twice."""
+    from kronmult_gb300 import workloads as W
+    from kronmult_gb300.api import forward_indexed
+
+    b = W.config5(scale=16 / 2048)
+    fac = torch.from_numpy(b.factors).to(cuda)
+    x = torch.from_numpy(b.inputs).to(cuda)
+    y = torch.zeros((b.n_out, b.N), dtype=torch.float64, device=cuda)
+    fidx = torch.from_numpy(b.fac_index[:, None] * b.d + np.arange(b.d)[None, :]).to(cuda).to(torch.int32)
+    oidx = torch.from_numpy(b.out_index).to(cuda).to(torch.int32)
+    st = torch.cuda.Stream(cuda)
+    with torch.cuda.stream(st):
+        scratch = forward_indexed(b.d, b.n, b.stride, fac, fidx, x, y, oidx, stream=st)  # warm-up, plans
+    torch.cuda.synchronize()
+    y.zero_()
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=st):
+        forward_indexed(b.d, b.n, b.stride, fac, fidx, x, y, oidx, scratch=scratch, stream=st)
+    g.replay()
+    g.replay()
+    torch.cuda.synchronize()
+    want = 2 * (O.forward(b) - b.out_init)
+    assert O.rel_l2(y.cpu().numpy(), want) <= 1e-13
