@@ -17,8 +17,12 @@ const DeviceInfo &device_info(int dev)
     DeviceInfo di;
     cudaDeviceGetAttribute(&di.sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&di.max_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaDeviceGetAttribute(&di.smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    cudaDeviceGetAttribute(&di.smem_reserved_cta, cudaDevAttrReservedSharedMemoryPerBlock, dev);
     if (di.sms <= 0) di.sms = 1;
     if (di.max_smem_optin <= 0) di.max_smem_optin = 48 * 1024;
+    if (di.smem_per_sm <= 0) di.smem_per_sm = di.max_smem_optin;
+    if (di.smem_reserved_cta < 0) di.smem_reserved_cta = 0;
     return cache.emplace(dev, di).first->second;
 }
 

@@ -13,7 +13,9 @@ namespace kgb {
 // per-device properties, queried once
 struct DeviceInfo {
     int sms = 0;
-    int max_smem_optin = 0;  // bytes of dynamic shared memory one CTA may opt into
+    int max_smem_optin = 0;      // bytes of dynamic shared memory one CTA may opt into
+    int smem_per_sm = 0;         // bytes of shared memory per SM
+    int smem_reserved_cta = 0;   // bytes the system reserves per resident CTA
 };
 
 const DeviceInfo &device_info(int dev);

@@ -361,11 +361,11 @@ int launch_tc_forward(int kind, int d, int n, const float *const *mats, int stri
     const size_t need = (size_t)2 * (a.N + d * 64) * sizeof(float) + (size_t)a.tiles * kTileBytes +
                         (size_t)d * kBBytes + 16;
     // resident CTAs per SM are limited so that their tensor-memory columns fit in 512:
-    // each CTA reserves at least 1/max_ctas of the SM's shared memory
+    // each CTA reserves 1/max_ctas of the SM's shared memory (less the per-CTA system
+    // reservation), so exactly max_ctas fit
     const int max_ctas = 512 / cols;
-    size_t smem = need;
-    const size_t per_sm = 228 * 1024;
-    if (smem * max_ctas < per_sm) smem = per_sm / max_ctas - 1024 + 16;
+    size_t smem = (size_t)di.smem_per_sm / max_ctas - (size_t)di.smem_reserved_cta;
+    smem &= ~(size_t)15;
     if (smem < need) smem = need;
     if (smem > (size_t)di.max_smem_optin) return cudaErrorNotSupported;
     const void *fn = kind == KRONMULT_COMPUTE_TF32 ? (const void *)fwd_tc_kernel<KIND_TF32>
