@@ -94,7 +94,8 @@ static int64_t ipow64(int64_t b, int e)
     int oracle_kronmult_batched_##SUF(int d, int n, const T *const *mats, int stride, T *const *in,    \
                                       T *const *out, int nb, int nthreads)                             \
     {                                                                                                  \
-        if (nb <= 0 || d <= 0 || n <= 0) return 0;                                                     \
+        /* d = 0 is the empty product (N = 1): out += in, as in the reference */                     \
+        if (nb <= 0 || d < 0 || n <= 0) return 0;                                                      \
         int64_t N = ipow64(n, d);                                                                      \
         int fail = 0;                                                                                  \
         int nt = nthreads > 0 ? nthreads : oracle_max_threads();                                       \
@@ -134,10 +135,10 @@ static int64_t ipow64(int64_t b, int e)
             free(K2);                                                                                  \
             return 2;                                                                                  \
         }                                                                                              \
-        int64_t s = n;                                                                                 \
-        for (int r = 0; r < n; r++)                                                                    \
-            for (int c = 0; c < n; c++) K[r + c * s] = mats[0][r + (int64_t)c * stride];               \
-        for (int m = 1; m < d; m++) {                                                                  \
+        /* start from the 1 x 1 identity, so that d = 0 gives out += in */                             \
+        int64_t s = 1;                                                                                 \
+        K[0] = (T)1;                                                                                   \
+        for (int m = 0; m < d; m++) {                                                                  \
             int64_t s2 = s * n;                                                                        \
             const T *A = mats[m];                                                                      \
             for (int64_t r1 = 0; r1 < s; r1++)                                                         \

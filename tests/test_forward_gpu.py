@@ -320,3 +320,16 @@ def test_forward_from_host_pipelines(cuda, chunks):
         fn(db, h_in, h_fac, h_out, chunks=chunks)
         torch.cuda.synchronize()
         assert O.rel_l2(h_out.numpy(), ref) <= TOL64
+
+
+@pytest.mark.parametrize("d,n", [(0, 3), (1, 1), (3, 1), (1, 2), (1, 8), (2, 9), (2, 12), (3, 10), (2, 16)])
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_edge_shapes(cuda, d, n, dtype):
+    """d = 0 (the empty product: output += input), n = 1, single factors, and n > 8
+    (the generic kernel) against the oracle."""
+    from kronmult_gb300 import workloads as W
+
+    b = W.make_batch(d, n, n + 2, 5, 3, seed=900 + 10 * d + n, out_init="normal")
+    got, _ = run(b, cuda, dtype=dtype)
+    tol = TOL64 if dtype == torch.float64 else TOL32
+    assert O.rel_l2(got, O.forward(b)) <= tol

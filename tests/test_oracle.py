@@ -62,3 +62,20 @@ def test_reference_naive_d1_agrees():
 def test_empty_batch_is_noop():
     b, z = load_golden("empty_batch")
     assert O.forward(b).shape == (0, b.N)
+
+
+@pytest.mark.parametrize("d,n", [(0, 3), (0, 1), (1, 1), (3, 1), (1, 2), (2, 9), (2, 12), (3, 10)])
+def test_edge_shapes_against_definition(d, n):
+    """d = 0 (the empty product, out += in), n = 1 and n > 8: the sweep against the
+    explicit Kronecker product, and against the reference build where it is present."""
+    from kronmult_gb300 import workloads as W
+
+    b = W.make_batch(d, n, n + 2, 5, 3, seed=930 + 10 * d + n, out_init="normal")
+    got = O.forward(b)
+    assert O.rel_l2(got, O.forward(b, impl="naive")) <= 1e-14
+    if d == 0:
+        want = b.out_init.copy()
+        np.add.at(want, b.out_index, b.inputs)
+        assert O.rel_l2(got, want) <= 1e-15  # only the order of the additions differs
+    if O.available("reference"):
+        assert O.rel_l2(got, O.forward(b, impl="reference")) <= 1e-15
