@@ -226,7 +226,9 @@ int kronmult_batched_f64_emulated_async(int matrix_count, int matrix_size, const
  * kronmult_batched interface are built on `stream` into caller-provided `scratch`
  * of at least kronmult_indexed_scratch_bytes(d, nb) bytes, then the regular forward
  * runs; nothing is allocated or synchronised.  Inputs are not modified (vectors
- * beyond shared memory are not supported here: cudaErrorNotSupported).
+ * beyond shared memory are not supported here: cudaErrorNotSupported).  As with
+ * the pointer arrays of kronmult_batched, the indices are not range-checked: every
+ * index must address a row inside its array.
  */
 long long kronmult_indexed_scratch_bytes(int matrix_count, int nb_batch);
 int kronmult_indexed_f64_async(int matrix_count, int matrix_size, int matrix_stride, const double *factors,

@@ -38,7 +38,8 @@ int indexed_async(int d, int n, int stride, const T *factors, long long factor_p
     if (nb == 0 || n == 0) return cudaSuccess;
     if (!factors && d > 0) return cudaErrorInvalidValue;
     if (!inputs || !outputs || !output_index || (d > 0 && !factor_index) || !scratch) return cudaErrorInvalidValue;
-    if (factor_pitch < (long long)stride * n || input_pitch < 0 || output_pitch < 0) return cudaErrorInvalidValue;
+    if ((d > 0 && factor_pitch < (long long)stride * n) || input_pitch < 0 || output_pitch < 0)
+        return cudaErrorInvalidValue;
     const size_t need = (size_t)nb * (size_t)(d + 2) * sizeof(void *);
     if (scratch_bytes < need || (reinterpret_cast<uintptr_t>(scratch) & 7u)) return cudaErrorInvalidValue;
     const T **mats = static_cast<const T **>(scratch);
