@@ -309,6 +309,21 @@ def suite_large(args, emit, reps):
         emit(f"large_n8_d6_b{nb}_{name}", _Shape(), total / reps, es, es,
              {"published_v100_ms": 221 if name == "f64" else 100, "source": "tests/bench_results.txt:12,42"})
         if name == "f64":
+            # FP64-accurate double-float emulation, two passes through the workspace
+            from kronmult_gb300.api import forward_f64_emulated
+
+            db.inputs.copy_(x0)
+            db.outputs.zero_()
+            db.forward(stream=st)
+            native = db.outputs.clone()
+            db.inputs.copy_(x0)
+            db.outputs.zero_()
+            forward_f64_emulated(db, stream=st)
+            torch.cuda.synchronize()
+            err = (torch.linalg.norm(db.outputs - native) / torch.linalg.norm(native)).item()
+            ms = _timed(lambda: forward_f64_emulated(db, stream=st), st, max(1, reps))
+            emit(f"large_n8_d6_b{nb}_f64_emulated", _Shape(), ms, 8, 8,
+                 {"rel_l2_vs_native_fp64": err, "published_v100_ms": 221})
             db.inputs.copy_(x0)
             ref = reference_gpu_ms(db, reps=1)
             if ref is not None:

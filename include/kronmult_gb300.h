@@ -210,11 +210,16 @@ int kronmult_diag_fp64_fma_gflops(double *gflops);
  * 1e-13 relative L2).  Per entry and per factor power-of-two scaling keeps any finite
  * input in range; values more than 2^126 below the largest of their vector or factor
  * count as zero.  Same semantics as kronmult_batched_f64_async otherwise (inputs not
- * modified).  Supports 2 <= n <= 8 with n^d fitting one team's shared memory.
+ * modified).  Supports 2 <= n <= 8.  Vectors beyond one team's shared memory need
+ * `workspace_batched` (N values per entry, overwritten): they run in two passes, the
+ * fastest tensor indices per contiguous chunk and the rest per tile of the workspace,
+ * each scaled by its own largest magnitude; without a workspace they return
+ * cudaErrorNotSupported.
  */
 int kronmult_batched_f64_emulated_async(int matrix_count, int matrix_size, const double *const *matrix_list_batched,
                                         int matrix_stride, const double *const *input_batched,
-                                        double *const *output_batched, int nb_batch, void *stream);
+                                        double *const *output_batched, double *const *workspace_batched,
+                                        int nb_batch, void *stream);
 
 /*
  * Indexed forward: integer maps instead of pointer arrays (the interface form

@@ -81,7 +81,7 @@ SIGNATURES = {
                                         ctypes.c_longlong, _vp, _i, _vp, ctypes.c_longlong, _vp]),
     "kronmult_indexed_f32_async": (_i, [_i, _i, _i, _vp, ctypes.c_longlong, _vp, _vp, ctypes.c_longlong, _vp, _vp,
                                         ctypes.c_longlong, _vp, _i, _vp, ctypes.c_longlong, _vp]),
-    "kronmult_batched_f64_emulated_async": (_i, [_i, _i, _vp, _i, _vp, _vp, _i, _vp]),
+    "kronmult_batched_f64_emulated_async": (_i, [_i, _i, _vp, _i, _vp, _vp, _vp, _i, _vp]),
     "kronmult_batched_f64_noalloc": (_i, [_i, _i, _vp, _i, _vp, _vp, _i, _vp]),
     "kronmult_diag_fp64_fma_gflops": (_i, [ctypes.POINTER(ctypes.c_double)]),
     "kronmult_pow_int": (ctypes.c_longlong, [_i, _i]),

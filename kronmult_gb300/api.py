@@ -353,8 +353,9 @@ def forward_f64_emulated(b: DeviceBatch, stream=None) -> None:
     (kronmult_batched_f64_emulated_async): FP64-accurate (relative error ~1e-14)."""
     if b.inputs.dtype != torch.float64 or b.outputs.dtype != torch.float64:
         raise TypeError("the emulated FP64 forward needs float64 factors, inputs and outputs")
+    ws = b.ws_ptrs.data_ptr() if b.ws_ptrs is not None else None
     st = _lib.lib().kronmult_batched_f64_emulated_async(b.d, b.n, b.mat_ptrs.data_ptr(), b.stride,
-                                                         b.in_ptrs.data_ptr(), b.out_ptrs.data_ptr(), b.nb,
+                                                         b.in_ptrs.data_ptr(), b.out_ptrs.data_ptr(), ws, b.nb,
                                                          _stream_handle(stream))
     _lib.check(st, "kronmult_batched_f64_emulated_async")
 

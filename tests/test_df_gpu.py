@@ -12,11 +12,11 @@ pytestmark = pytest.mark.gpu
 TOL64 = 1e-13
 
 
-def run_df(b, cuda):
+def run_df(b, cuda, ws=False):
     from kronmult_gb300 import DeviceBatch
     from kronmult_gb300.api import forward_f64_emulated
 
-    db = DeviceBatch.from_host(b, device=cuda)
+    db = DeviceBatch.from_host(b, device=cuda, with_workspace=ws)
     forward_f64_emulated(db)
     torch.cuda.synchronize()
     return db.outputs.cpu().numpy()
@@ -65,3 +65,44 @@ def test_df_zeros_and_nonfinite(cuda):
     assert np.array_equal(got[0], want[0])  # zero vector -> zero contribution
     assert not np.isfinite(got[1]).all() and not np.isfinite(want[1]).all()
     assert O.rel_l2(got[2], want[2]) <= TOL64
+
+
+@pytest.mark.parametrize("d,n,stride", [(5, 8, 8), (10, 3, 4), (8, 4, 5), (7, 5, 5), (16, 2, 2), (7, 6, 6), (5, 7, 7)])
+def test_df_two_pass(cuda, d, n, stride):
+    """Vectors beyond one team's shared memory: two passes through the workspace,
+    chunks and tiles each with their own power-of-two scale."""
+    from kronmult_gb300 import DeviceBatch
+    from kronmult_gb300 import workloads as W
+
+    b = W.make_batch(d, n, stride, 3, 2, seed=760 + 10 * d + n, out_init="normal")
+    db = DeviceBatch.from_host(b, device=cuda, with_workspace=True)
+    x0 = db.inputs.clone()
+    from kronmult_gb300.api import forward_f64_emulated
+
+    forward_f64_emulated(db)
+    torch.cuda.synchronize()
+    assert O.rel_l2(db.outputs.cpu().numpy(), O.forward(b)) <= TOL64
+    assert torch.equal(db.inputs, x0)
+
+
+def test_df_two_pass_published_shape_wide_range(cuda):
+    """The published n = 8, d = 6 shape (stride 67, 5 aliased outputs) with inputs
+    spanning 2^-300 .. 2^300 across entries and positions."""
+    from kronmult_gb300 import workloads as W
+
+    b = W.make_batch(6, 8, 67, 5, 2, seed=3904)
+    rng = np.random.Generator(np.random.PCG64(3905))
+    b.inputs = b.inputs * np.exp2(rng.integers(-300, 300, size=(b.nb, 1)))
+    assert O.rel_l2(run_df(b, cuda, ws=True), O.forward(b)) <= TOL64
+
+
+def test_df_large_without_workspace_is_not_supported(cuda):
+    from kronmult_gb300 import DeviceBatch
+    from kronmult_gb300 import workloads as W
+    from kronmult_gb300.api import forward_f64_emulated
+    from kronmult_gb300._lib import KronmultError
+
+    b = W.make_batch(5, 8, 8, 1, 1, seed=3906)
+    db = DeviceBatch.from_host(b, device=cuda)
+    with pytest.raises(KronmultError):
+        forward_f64_emulated(db)
