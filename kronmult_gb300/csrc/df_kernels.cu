@@ -146,6 +146,7 @@ template <int NN, int QMAX> __global__ void __launch_bounds__(256, 3) df_single_
     __shared__ int s_emax[256 / 8 * 32];  // per team: vector scale + reduction space (<= 32 slots)
     const Team tm(a.team_size);
     constexpr int NN2 = NN * NN;
+    constexpr bool kSwz = VecSwizzle<float, NN>::on;  // staged hi / lo vectors (n = 8: swizzled)
     float *xh = reinterpret_cast<float *>(smem_raw) + (size_t)tm.id * a.team_elems;
     float *xl = xh + a.vpad;
     float *mh = xl + a.vpad;                 // d * NN2
@@ -170,7 +171,10 @@ template <int NN, int QMAX> __global__ void __launch_bounds__(256, 3) df_single_
     }
     tm.sync();
     // ---- split into hi/lo floats
-    for (int v = tm.rank; v < N; v += tm.size) df_split(x[v], xe, xh[v], xl[v]);
+    for (int v = tm.rank; v < N; v += tm.size) {
+        const int p = vec_pos<float, kSwz>(v);
+        df_split(x[v], xe, xh[p], xl[p]);
+    }
     for (int idx = tm.rank; idx < d * NN2; idx += tm.size) {
         const int i = idx / NN2, rem = idx - i * NN2, k = rem / NN, r = rem - k * NN;
         df_split(mats[i][r + (size_t)k * a.stride], fexp[i], mh[idx], ml[idx]);
@@ -186,12 +190,12 @@ template <int NN, int QMAX> __global__ void __launch_bounds__(256, 3) df_single_
         for (int q = 0; q < QMAX; ++q) {
             const int c = tm.rank + q * tm.size;
             if (c < F) {
+                // whole-fibre vector loads (16-byte for n = 4, 8; the swizzled layout
+                // for n = 8): consecutive lanes read consecutive fibres without bank
+                // conflicts
                 float bh[NN], bl[NN];
-#pragma unroll
-                for (int k = 0; k < NN; ++k) {
-                    bh[k] = xh[k + c * NN];
-                    bl[k] = xl[k + c * NN];
-                }
+                load_fibre_v<float, NN, kSwz>(xh, c, bh);
+                load_fibre_v<float, NN, kSwz>(xl, c, bl);
                 df_fibre<NN>(Mh, Ml, bh, bl, yh[q], yl[q]);
             }
         }
@@ -203,8 +207,9 @@ template <int NN, int QMAX> __global__ void __launch_bounds__(256, 3) df_single_
                 if (c < F) {
 #pragma unroll
                     for (int r = 0; r < NN; ++r) {
-                        xh[c + r * F] = yh[q][r];
-                        xl[c + r * F] = yl[q][r];
+                        const int p = vec_pos<float, kSwz>(c + r * F);
+                        xh[p] = yh[q][r];
+                        xl[p] = yl[q][r];
                     }
                 }
             }
@@ -240,6 +245,7 @@ template <int NN, int QMAX> __global__ void __launch_bounds__(256, 3) df_pass1_k
     __shared__ int s_emax[256 / 8 * 32];
     const Team tm(a.team_size);
     constexpr int NN2 = NN * NN;
+    constexpr bool kSwz = VecSwizzle<float, NN>::on;
     const int C = a.C, F = C / NN, d1 = a.d1, d2 = a.d - d1;
     float *xh = reinterpret_cast<float *>(smem_raw) + (size_t)tm.id * a.team_elems;
     float *xl = xh + a.vpad;
@@ -263,7 +269,10 @@ template <int NN, int QMAX> __global__ void __launch_bounds__(256, 3) df_pass1_k
         fexp[i] = fm;
     }
     tm.sync();
-    for (int v = tm.rank; v < C; v += tm.size) df_split(x[v], xe, xh[v], xl[v]);
+    for (int v = tm.rank; v < C; v += tm.size) {
+        const int p = vec_pos<float, kSwz>(v);
+        df_split(x[v], xe, xh[p], xl[p]);
+    }
     for (int idx = tm.rank; idx < d1 * NN2; idx += tm.size) {
         const int i = idx / NN2, rem = idx - i * NN2, k = rem / NN, r = rem - k * NN;
         df_split(mats[i][r + (size_t)k * a.stride], fexp[i], mh[idx], ml[idx]);
@@ -278,12 +287,12 @@ template <int NN, int QMAX> __global__ void __launch_bounds__(256, 3) df_pass1_k
         for (int q = 0; q < QMAX; ++q) {
             const int c = tm.rank + q * tm.size;
             if (c < F) {
+                // whole-fibre vector loads (16-byte for n = 4, 8; the swizzled layout
+                // for n = 8): consecutive lanes read consecutive fibres without bank
+                // conflicts
                 float bh[NN], bl[NN];
-#pragma unroll
-                for (int k = 0; k < NN; ++k) {
-                    bh[k] = xh[k + c * NN];
-                    bl[k] = xl[k + c * NN];
-                }
+                load_fibre_v<float, NN, kSwz>(xh, c, bh);
+                load_fibre_v<float, NN, kSwz>(xl, c, bl);
                 df_fibre<NN>(Mh, Ml, bh, bl, yh[q], yl[q]);
             }
         }
@@ -295,8 +304,9 @@ template <int NN, int QMAX> __global__ void __launch_bounds__(256, 3) df_pass1_k
                 if (c < F) {
 #pragma unroll
                     for (int r = 0; r < NN; ++r) {
-                        xh[c + r * F] = yh[q][r];
-                        xl[c + r * F] = yl[q][r];
+                        const int p = vec_pos<float, kSwz>(c + r * F);
+                        xh[p] = yh[q][r];
+                        xl[p] = yl[q][r];
                     }
                 }
             }
