@@ -352,16 +352,26 @@ __global__ void __launch_bounds__(512) adj_smem_kernel(const AdjArgs<T> a)
                     }
                     pi = src;
                 }
-                // partial G_(i) P_(i)^T over slices of t
+                // partial G_(i) P_(i)^T over slices of t: items (row r, slice); an item
+                // reads G(r, t) once and the whole fibre P(:, t) with vector loads and
+                // keeps a row of NN sums in registers
                 const int S = a.slices;
                 const int tlen = (R + S - 1) / S;
-                for (int w = tm.rank; w < S * P; w += tm.size) {
-                    const int pr = w % P, sl = w / P;
-                    const int r = pr % NN, c = pr / NN;
+                for (int w = tm.rank; w < S * NN; w += tm.size) {
+                    const int r = w % NN, sl = w / NN;
                     const int t0 = sl * tlen, t1 = min(R, t0 + tlen);
-                    T s = T(0);
-                    for (int t = t0; t < t1; ++t) s = fma_t<T>(qb[t + R * r], pi[c + NN * t], s);
-                    gpart[w] = s;
+                    T s[NN];
+#pragma unroll
+                    for (int c = 0; c < NN; ++c) s[c] = T(0);
+                    for (int t = t0; t < t1; ++t) {
+                        const T gv = qb[t + R * r];
+                        T pv[NN];
+                        load_fibre<T, NN>(pi + NN * t, pv);
+#pragma unroll
+                        for (int c = 0; c < NN; ++c) s[c] = fma_t<T>(gv, pv[c], s[c]);
+                    }
+#pragma unroll
+                    for (int c = 0; c < NN; ++c) gpart[sl * P + r + NN * c] = s[c];
                 }
                 tm.sync();
                 for (int pr = tm.rank; pr < P; pr += tm.size) {

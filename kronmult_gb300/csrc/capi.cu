@@ -115,7 +115,7 @@ static int adjoint_async(int d, int n, const T *const *mats, int stride, const T
         int qmax = 1;
         while (qmax < q) qmax *= 2;
         if (qmax <= 4) fn = adj_fibre_lookup<T>(n, qmax);
-        slices = ts / P;
+        slices = ts / n;  // gradient contraction items: (row, slice of t)
     }
     if (!fn) {
         // element-mapped phases: pick the team whose lanes are best used over N outputs
