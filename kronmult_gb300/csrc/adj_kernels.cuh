@@ -275,8 +275,9 @@ __device__ __forceinline__ void mode_slow_inplace(T *buf, const T *M, int R, con
     tm.sync();
 }
 
+// teams of at most 256 threads; 80 registers, 3 CTAs per SM
 template <typename T, int NN, int QMAX>
-__global__ void __launch_bounds__(512) adj_smem_kernel(const AdjArgs<T> a)
+__global__ void __launch_bounds__(256, 3) adj_smem_kernel(const AdjArgs<T> a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const Team tm(a.team_size);

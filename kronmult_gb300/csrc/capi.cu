@@ -108,13 +108,14 @@ static int adjoint_async(int d, int n, const T *const *mats, int stride, const T
             ts = tune->team_size;
             if (ts < 8 || ts > 512 || (ts & (ts - 1))) return cudaErrorInvalidValue;
         } else {
-            while (ts < 512 && ts * 2 < R) ts *= 2;
+            while (ts < 256 && ts * 2 < R) ts *= 2;
         }
-        while (ts < 512 && (R + ts - 1) / ts > 4) ts *= 2;
+        while (ts < 256 && (R + ts - 1) / ts > 4) ts *= 2;
         const int q = (R + ts - 1) / ts;
         int qmax = 1;
         while (qmax < q) qmax *= 2;
-        if (qmax <= 4) fn = adj_fibre_lookup<T>(n, qmax);
+        // the fibre-mapped kernel runs teams of at most 256 threads (else element-mapped)
+        if (qmax <= 4 && ts <= 256) fn = adj_fibre_lookup<T>(n, qmax);
         slices = ts / n;  // gradient contraction items: (row, slice of t)
     }
     if (!fn) {
