@@ -442,6 +442,19 @@ def suite(args):
         ms = _timed(lambda: graph.replay(), torch.cuda.current_stream(), reps)
         emit(f"c3_grouped_{mode}_graph_f64", groups, ms, 8, 8, {"plan": plan.info()})
         plan.close()
+        # the same with per-group team sizes picked by timing the persistent kernel
+        tunings = G.autotune_grouped(dbs, mode=mode, stream=st)
+        plan = G.GroupedPlan(dbs, mode=mode, tunings=tunings)
+        with torch.cuda.stream(st):
+            plan.run(stream=st)
+        torch.cuda.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=st):
+            plan.run(stream=st)
+        ms = _timed(lambda: graph.replay(), torch.cuda.current_stream(), reps)
+        emit(f"c3_grouped_{mode}_autotuned_graph_f64", groups, ms, 8, 8,
+             {"plan": plan.info(), "team_sizes": [t.get("team_size", 0) for t in tunings]})
+        plan.close()
     del dbs
     torch.cuda.empty_cache()
 

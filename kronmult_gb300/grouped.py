@@ -8,6 +8,8 @@ result is bitwise reproducible.
 
 `autotune_forward(d, n, dtype)` times the forward's launch shapes on the GPU and
 stores the fastest in the library's tuning cache, which the planners consult.
+`autotune_grouped(batches, mode)` picks a team size per group for the persistent
+kernel itself and returns the tunings to pass to GroupedPlan.
 """
 from __future__ import annotations
 
@@ -82,6 +84,47 @@ def autotune_forward(d: int, n: int, dtype: int = _lib.KRONMULT_DTYPE_F64, nb_sa
     _lib.check(_lib.lib().kronmult_autotune_forward(d, n, dtype, nb_sample, ctypes.byref(t), ctypes.byref(ms)),
                "kronmult_autotune_forward")
     return _as_dict(t), ms.value
+
+
+def autotune_grouped(batches: list[DeviceBatch], mode: str = "atomic",
+                     team_sizes=(0, 8, 16, 32, 64, 128, 256), reps: int = 5, stream=None) -> list[dict]:
+    """Per-group tunings for GroupedPlan: for every group, a one-group plan of the
+    persistent kernel is timed (CUDA events, `reps` launches after one warm-up) with
+    each candidate team size (0 = the planner's own choice), and the fastest is kept.
+    The groups' outputs are restored afterwards.  Returns one tuning dict per group."""
+    st = stream or torch.cuda.current_stream()
+    tunings = []
+    for b in batches:
+        saved = b.outputs.clone()
+        best, best_ms, seen = {}, float("inf"), set()
+        for ts in team_sizes:
+            t = {"team_size": int(ts)} if ts else {}
+            try:
+                plan = GroupedPlan([b], mode=mode, tunings=[t])
+            except _lib.KronmultError:
+                continue
+            info = plan.info()
+            shape = (info["block"], info["smem"], info["items"], info["ranges"])
+            if shape in seen:  # a forced size the planner grew into an already timed shape
+                plan.close()
+                continue
+            seen.add(shape)
+            plan.run(stream=st)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            for _ in range(reps):
+                plan.run(stream=st)
+            e1.record(st)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            plan.close()
+            if ms < best_ms:
+                best, best_ms = t, ms
+        b.outputs.copy_(saved)
+        tunings.append(best)
+    torch.cuda.synchronize()
+    return tunings
 
 
 def tuning_cache_get(d: int, n: int, dtype: int = _lib.KRONMULT_DTYPE_F64):

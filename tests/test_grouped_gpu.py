@@ -156,3 +156,24 @@ def test_autotune_and_cache(cuda, tmp_path):
     db.forward(sync=True)  # uses the cached shape
     assert O.rel_l2(db.outputs.cpu().numpy(), O.forward(b)) <= TOL64
     G.tuning_cache_clear()
+
+
+def test_autotune_grouped_tunings_give_correct_results(cuda):
+    """Per-group team sizes picked by timing the persistent kernel; the plan built
+    with them matches the oracle and the outputs are left as they were by the search."""
+    from kronmult_gb300 import DeviceBatch
+    from kronmult_gb300 import grouped as G
+    from kronmult_gb300 import workloads as W
+
+    groups = W.config3(scale=40 / 8000)
+    dbs = [DeviceBatch.from_host(b, device=cuda) for b in groups]
+    tunings = G.autotune_grouped(dbs, mode="atomic", reps=2)
+    assert len(tunings) == len(groups)
+    for db, b in zip(dbs, groups):
+        assert torch.equal(db.outputs.cpu(), torch.from_numpy(b.out_init))
+    plan = G.GroupedPlan(dbs, mode="atomic", tunings=tunings)
+    plan.run()
+    torch.cuda.synchronize()
+    for db, b in zip(dbs, groups):
+        assert O.rel_l2(db.outputs.cpu().numpy(), O.forward(b)) <= 1e-13
+    plan.close()
