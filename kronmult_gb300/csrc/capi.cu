@@ -108,7 +108,9 @@ static int adjoint_async(int d, int n, const T *const *mats, int stride, const T
             ts = tune->team_size;
             if (ts < 8 || ts > 512 || (ts & (ts - 1))) return cudaErrorInvalidValue;
         } else {
-            while (ts < 256 && ts * 2 < R) ts *= 2;
+            // up to 4 fibres per thread: smaller teams, more entries in flight per SM
+            // (measured faster than 2 per thread on d = 3, n = 6)
+            while (ts < 256 && ts * 4 < R) ts *= 2;
         }
         while (ts < 256 && (R + ts - 1) / ts > 4) ts *= 2;
         const int q = (R + ts - 1) / ts;
