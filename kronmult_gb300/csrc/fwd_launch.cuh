@@ -218,8 +218,10 @@ int plan_forward(FwdPlan<T, TO> &pl, int d, int n, const T *const *mats, int str
             ts = tune->team_size;
             while (ts < 512 && (F + ts - 1) / ts > qcap) ts *= 2;
         } else {
-            // smallest team that leaves every thread at most ~2-4 fibres
-            const int qtarget = (n <= 4) ? 4 : 2;
+            // smallest team that leaves every thread at most ~2-4 fibres (4 for FP64
+            // n = 6 too: smaller teams keep more entries in flight, measured 5-25 %
+            // faster on d = 2..4)
+            const int qtarget = (n <= 4 || (n == 6 && sizeof(T) == 8)) ? 4 : 2;
             while (ts < 512 && (long long)ts * qtarget < F) ts *= 2;
         }
         // One entry per team (fwd_single_kernel) unless runs are requested: measured
@@ -245,10 +247,12 @@ int plan_forward(FwdPlan<T, TO> &pl, int d, int n, const T *const *mats, int str
             int teams = 256 / ts;
             auto fn = fwd_single_lookup<T, TO>(n, qmax);
             // whole fibres per thread leave (ts*qmax - F) of ts*qmax slots idle; when that
-            // is more than a tenth, map output elements to threads instead (FP64 only:
-            // for FP32 the fibre's register reuse is worth more)
+            // is more than a tenth, map output elements to threads instead -- FP64 with
+            // odd n only (n = 3, 5, 7: fibres of 8-byte loads).  For FP32, and for FP64
+            // fibres of 16-byte loads (n = 6: measured up to 34 % faster than elements),
+            // the fibre's register reuse is worth more.
             const double fibre_util = (double)F / ((double)ts * ((F + ts - 1) / ts));
-            if (sizeof(T) == 8 && fibre_util < 0.9 && !(tune && tune->team_size > 0)) {
+            if (sizeof(T) == 8 && (n & 1) && fibre_util < 0.9 && !(tune && tune->team_size > 0)) {
                 const int best_ts = elem_team_size(N, 16, 0, 256);
                 const double best =
                     best_ts ? (double)N / ((double)best_ts * ((N + best_ts - 1) / best_ts)) : 0.0;
