@@ -22,7 +22,7 @@ template <typename T, typename TO> struct FwdArgs {
     const T *const *mats;  // nb*d factor pointers, entry k's factors at [k*d, k*d+d)
     const T *const *in;    // nb input pointers (N values each)
     TO *const *out;        // nb output pointers (may alias)
-    T *const *ws;          // nb workspace pointers (generic global path only; may be null)
+    T *const *ws;          // nb workspace pointers (global-memory paths only; may be null)
     long long nb;          // number of entries
     int d, n, stride;      // factor count, factor size, factor leading dimension
     int N;                 // n^d
@@ -688,10 +688,10 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) fwd_single_kernel
 }
 
 // One entry per team with output elements (not whole fibres) mapped to threads,
-// runtime n: every lane has work for any n.  Selected for FP64 when the fibre
-// mapping would leave more than a tenth of the lanes idle (for example n = 6:
-// 36 fibres per mode on 32-lane teams), since the FP64 pipe is charged per warp
-// instruction whatever the number of active lanes.
+// runtime n: every lane has work for any n.  Selected for FP64 with odd n when the
+// fibre mapping would leave more than a tenth of the lanes idle (for example n = 7,
+// d = 3: 49 fibres per mode on 16-lane teams), since the FP64 pipe is charged per
+// warp instruction whatever the number of active lanes.
 template <typename T, typename TO, int EMAX>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) fwd_single_elem_kernel(const FwdArgs<T, TO> a)
 {
