@@ -93,9 +93,13 @@ int autotune_impl(int d, int n, int dtype, int nb_sample, kronmult_tuning *best,
             const int q = (F + ts - 1) / ts;
             if (q > qcap) continue;
             if (ts > 8 && (F + ts / 2 - 1) / (ts / 2) == 1 && ts > F) continue;  // larger teams only idle
-            for (int cand = 0; cand < 6; ++cand) {
+            // staging: two slots in place (2), one slot (1), and for factors read from
+            // shared memory the ping-pong buffers (3)
+            const int nstage = FactorInSmemHost<T>(n) ? 3 : 2;
+            for (int cand = 0; cand < 3 * nstage; ++cand) {
                 const int ept = (cand % 3 == 0) ? 0 : (cand % 3 == 1 ? 2 : 8);
-                kronmult_tuning t{ts, 0, ept, cand < 3 ? 2 : 1};
+                const int stage = cand / 3;  // 0, 1, 2 -> prefetch 2, 1, 3
+                kronmult_tuning t{ts, 0, ept, stage == 0 ? 2 : (stage == 1 ? 1 : 3)};
                 FwdPlan<T, TO> pl;
                 if (plan_forward<T, TO>(pl, d, n, mats, n, in, out, nullptr, nb, &t) != cudaSuccess) continue;
                 if (!pl.smem_path) continue;
@@ -184,7 +188,7 @@ int kronmult_tuning_cache_get(int matrix_count, int matrix_size, int dtype, kron
 
 int kronmult_tuning_cache_set(int matrix_count, int matrix_size, int dtype, const kronmult_tuning *t)
 {
-    if (!t || t->team_size < 0 || t->ctas_per_sm < 0 || t->entries_per_team < 0 || t->prefetch < 0 || t->prefetch > 2)
+    if (!t || t->team_size < 0 || t->ctas_per_sm < 0 || t->entries_per_team < 0 || t->prefetch < 0 || t->prefetch > 3)
         return cudaErrorInvalidValue;
     tuning_cache_store(matrix_count, matrix_size, dtype, *t);
     return cudaSuccess;

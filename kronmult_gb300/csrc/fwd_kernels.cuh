@@ -406,6 +406,120 @@ __device__ __forceinline__ void team_forward(const T *const *mats, const T *cons
     if (cur != nullptr) flush(cur);
 }
 
+// Ping-pong variant of team_forward (same run / deterministic semantics) for
+// factors read from shared memory: every mode reads one vector buffer and writes
+// the other, so a thread stores each output fibre as soon as it is computed -- one
+// barrier per mode instead of two, and no register array of all of the thread's
+// mode outputs besides the run sums.  Three vector buffers: the two of the entry
+// being computed and the one the next entry streams into (cp.async).
+template <typename T, typename TO, int NN, int QMAX, bool DET>
+__device__ __forceinline__ void team_forward_pp(const T *const *mats, const T *const *in, TO *const *out, int d,
+                                                int stride, int N, long long e_begin, long long e_end, T *vb0,
+                                                T *vb1, T *vb2, T *fb0, T *fb1, const Team &tm)
+{
+    const int F = N / NN;
+    constexpr bool kSwz = VecSwizzle<T, NN>::on;
+    T acc[QMAX][NN];
+    TO *cur = nullptr;
+    auto flush = [&](TO *dst) {
+#pragma unroll
+        for (int q = 0; q < QMAX; ++q) {
+            const int c = tm.rank + q * tm.size;
+            if (c < F) {
+#pragma unroll
+                for (int r = 0; r < NN; ++r) {
+                    if constexpr (DET) {
+                        dst[c + r * F] = dst[c + r * F] + (TO)acc[q][r];
+                    } else {
+                        atomic_add<TO>(dst + c + r * F, (TO)acc[q][r]);
+                    }
+                }
+            }
+        }
+    };
+    T *vcur = vb0, *vpp = vb1, *vnxt = vb2;
+    T *fcur = fb0, *fnxt = fb1;
+    if (e_begin < e_end) stage_async<T, NN, kSwz>(vcur, fcur, in[e_begin], mats + e_begin * d, N, d, stride, tm);
+    // highest rank in this thread's warp: the pair / single choice below is warp-uniform
+    const int last = tm.size < 32 ? tm.size - 1 : (tm.rank | 31);
+    for (long long e = e_begin; e < e_end; ++e) {
+        TO *o = out[e];
+        cp_async_wait_all();
+        tm.sync();  // entry e staged for the whole team; entry e-1 done with every buffer
+        if (e + 1 < e_end)
+            stage_async<T, NN, kSwz>(vnxt, fnxt, in[e + 1], mats + (e + 1) * d, N, d, stride, tm);
+        const bool fresh = o != cur;
+        if (fresh) {
+            if (cur != nullptr) flush(cur);
+            cur = o;
+        }
+        const T *src = vcur;
+        T *dst = vpp;
+        for (int i = d - 1; i >= 0; --i) {
+            const T *M = fcur + i * NN * NN;
+#pragma unroll
+            for (int q = 0; q < QMAX; q += 2) {
+                const int c0 = tm.rank + q * tm.size;
+                bool pair = false;
+                if constexpr (QMAX >= 2) pair = last + (q + 1) * tm.size < F;
+                if (pair) {
+                    if constexpr (QMAX >= 2) {
+                        T x0[NN], x1[NN], y0[NN], y1[NN];
+                        load_fibre_v<T, NN, kSwz>(src, c0, x0);
+                        load_fibre_v<T, NN, kSwz>(src, c0 + tm.size, x1);
+                        mode_fibre2_smem<T, NN>(M, x0, x1, y0, y1);
+                        if (i > 0) {
+#pragma unroll
+                            for (int r = 0; r < NN; ++r) {
+                                dst[vec_pos<T, kSwz>(c0 + r * F)] = y0[r];
+                                dst[vec_pos<T, kSwz>(c0 + tm.size + r * F)] = y1[r];
+                            }
+                        } else {
+#pragma unroll
+                            for (int r = 0; r < NN; ++r) {
+                                acc[q][r] = fresh ? y0[r] : acc[q][r] + y0[r];
+                                acc[q + 1][r] = fresh ? y1[r] : acc[q + 1][r] + y1[r];
+                            }
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int h = 0; h < (QMAX >= 2 ? 2 : 1); ++h) {
+                        const int c = c0 + h * tm.size;
+                        if (c < F) {
+                            T x0[NN], y0[NN];
+                            load_fibre_v<T, NN, kSwz>(src, c, x0);
+                            mode_fibre_smem<T, NN>(M, x0, y0);
+                            if (i > 0) {
+#pragma unroll
+                                for (int r = 0; r < NN; ++r) dst[vec_pos<T, kSwz>(c + r * F)] = y0[r];
+                            } else {
+#pragma unroll
+                                for (int r = 0; r < NN; ++r)
+                                    acc[q + h][r] = fresh ? y0[r] : acc[q + h][r] + y0[r];
+                            }
+                        }
+                    }
+                }
+            }
+            if (i > 0) {
+                tm.sync();  // mode outputs complete; every read of src done
+                T *t = const_cast<T *>(src);
+                src = dst;
+                dst = t;
+            }
+        }
+        T *t = vcur;  // the next entry's buffer becomes current; the old one is the next target
+        vcur = vnxt;
+        vnxt = t;
+        t = fcur;
+        fcur = fnxt;
+        fnxt = t;
+    }
+    if (cur != nullptr) flush(cur);
+    cp_async_wait_all();
+}
+
 // FP32 variants are capped at 64 registers so that four 256-thread CTAs fit on an SM
 // Element-mapped team forward with run accumulation (runtime n): thread `rank`
 // owns output elements q = rank + j*team_size (j < EMAX) of every mode, so all lanes
@@ -628,6 +742,15 @@ __global__ void __launch_bounds__(512, sizeof(T) == 4 ? 2 : 1) fwd_smem_kernel(c
     const long long team_global = (long long)blockIdx.x * a.teams_per_cta + tm.id;
     const long long e = team_global * a.entries_per_team;
     const long long e_end = min(e + (long long)a.entries_per_team, a.nb);
+    if constexpr (FactorInSmem<T, NN>::value) {
+        if (a.prefetch == 3) {  // ping-pong: three vector buffers, then two factor slots
+            T *vb1 = buf + a.vec_pad, *vb2 = vb1 + a.vec_pad;
+            T *fb0 = vb2 + a.vec_pad, *fb1 = fb0 + a.fac_pad;
+            team_forward_pp<T, TO, NN, QMAX, false>(a.mats, a.in, a.out, a.d, a.stride, a.N, e, e_end, buf, vb1,
+                                                     vb2, fb0, fb1, tm);
+            return;
+        }
+    }
     if (a.prefetch) {
         T *buf2 = fac + a.fac_pad;
         T *fac2 = buf2 + a.vec_pad;

@@ -38,6 +38,9 @@ inline long long pow_ll(int b, int e)
 
 inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
 
+// host twin of FactorInSmem: an n x n factor of T does not fit the register path
+template <typename T> inline bool FactorInSmemHost(int n) { return (size_t)n * n * sizeof(T) > 128; }
+
 // Team size (power of two, 8..max_ts) for an element-mapped kernel over N outputs:
 // the best lane utilisation N / (ts * ceil(N / ts)) with at most max_per outputs per
 // thread; among teams within 2 % of the best, the one closest to 8 outputs per thread.
@@ -334,10 +337,19 @@ int plan_forward(FwdPlan<T, TO> &pl, int d, int n, const T *const *mats, int str
             const int vpad = round_up(N, 16 / (int)sizeof(T));
             const int fpad = round_up(d * n * n, 16 / (int)sizeof(T));
             // two staging slots (asynchronous prefetch of the next entry) unless disabled
-            // or too large for a quarter of the SM's shared memory
+            // or too large for half of the SM's shared memory; FP32 with factors in
+            // shared memory (n >= 6) ping-pongs between vector buffers instead (three
+            // vector buffers, two factor slots)
             int prefetch = (tune && tune->prefetch == 1) ? 0 : 1;
             if ((size_t)2 * (vpad + fpad) * sizeof(T) > (size_t)di.max_smem_optin / 2) prefetch = 0;
-            const int team_elems = (prefetch ? 2 : 1) * (vpad + fpad);
+            const bool pp_ok = FactorInSmemHost<T>(n) && (size_t)(3 * vpad + 2 * fpad) * sizeof(T) <=
+                                                             (size_t)di.max_smem_optin / 2;
+            // default for FP32 into FP32 outputs (measured 1.5-4.5 % faster on n = 6, 8);
+            // with FP64 outputs the in-place slots measured faster
+            if (pp_ok && ((tune && tune->prefetch == 3) ||
+                          (sizeof(T) == 4 && sizeof(TO) == 4 && (!tune || tune->prefetch == 0))))
+                prefetch = 3;
+            const int team_elems = prefetch == 3 ? 3 * vpad + 2 * fpad : (prefetch ? 2 : 1) * (vpad + fpad);
             const size_t team_bytes = (size_t)team_elems * sizeof(T);
             int block = ts >= 256 ? ts : 256;
             int teams = block / ts;
