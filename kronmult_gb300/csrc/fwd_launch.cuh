@@ -222,7 +222,7 @@ int plan_forward(FwdPlan<T, TO> &pl, int d, int n, const T *const *mats, int str
             while (ts < 512 && (F + ts - 1) / ts > qcap) ts *= 2;
         } else {
             // smallest team that leaves every thread at most ~2-4 fibres (4 for FP64
-            // n = 6 too: smaller teams keep more entries in flight, measured 5-25 %
+            // n = 6 too: smaller teams keep more entries in flight, measured 5-34 %
             // faster on d = 2..4)
             const int qtarget = (n <= 4 || (n == 6 && sizeof(T) == 8)) ? 4 : 2;
             while (ts < 512 && (long long)ts * qtarget < F) ts *= 2;
