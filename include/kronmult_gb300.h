@@ -200,6 +200,13 @@ int kronmult_batched_f64_noalloc(int matrix_count, int matrix_size, const double
  * kernel left early (its outputs are then incomplete).  No reference counterpart. */
 int kronmult_device_error(int *code, int clear);
 
+/* Diagnostic: runs one CTA that waits, with the tensor-core kernels' bounded wait and
+ * a short limit, on an mbarrier that nothing arrives on; the wait runs out and records
+ * error code 1, which is returned in *code (expected: 1) and then cleared.  Shows
+ * that a wait that never completes ends in an error status, not a hang, and leaves
+ * the context usable.  Synchronises the device.  No reference counterpart. */
+int kronmult_diag_wait_selftest(int *code);
+
 /* Diagnostic: measured FP64 FMA throughput of the current GPU in GFLOP/s (no
  * reference counterpart).  Allocates and synchronises; not for use in a graph. */
 int kronmult_diag_fp64_fma_gflops(double *gflops);

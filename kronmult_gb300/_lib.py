@@ -75,6 +75,7 @@ SIGNATURES = {
     "kronmult_tuning_cache_save": (_i, [ctypes.c_char_p]),
     "kronmult_tuning_cache_load": (_i, [ctypes.c_char_p]),
     "kronmult_device_error": (_i, [ctypes.POINTER(ctypes.c_int), _i]),
+    "kronmult_diag_wait_selftest": (_i, [ctypes.POINTER(ctypes.c_int)]),
     "kronmult_indexed_scratch_bytes": (ctypes.c_longlong, [_i, _i]),
     "kronmult_host_device_pointer": (_i, [_vp, ctypes.POINTER(ctypes.c_void_p)]),
     "kronmult_indexed_f64_async": (_i, [_i, _i, _i, _vp, ctypes.c_longlong, _vp, _vp, ctypes.c_longlong, _vp, _vp,

@@ -90,9 +90,9 @@ __device__ __forceinline__ void mma_commit(uint32_t mbar)
                  : "memory");
 }
 
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase)
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase, unsigned limit = kWaitLimit)
 {
-    for (unsigned it = 0; it < kWaitLimit; ++it) {
+    for (unsigned it = 0; it < limit; ++it) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
@@ -387,7 +387,39 @@ int launch_tc_forward(int kind, int d, int n, const float *const *mats, int stri
     return (int)cudaGetLastError();
 }
 
+// Self-test of the bounded wait: an mbarrier that nothing ever arrives on is waited
+// for with the kernels' own bounded wait (a short limit); the wait runs out, the
+// kernel records code 1 in the device error word and returns, and the context stays
+// usable.  No tensor memory, no copies in flight.
+__global__ void wait_selftest_kernel()
+{
+    __shared__ uint64_t mbar;
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const bool ok = mbar_wait(smem_u32(&mbar), 0, 1u << 12);
+    if (__syncthreads_or(!ok) && threadIdx.x == 0) atomicCAS(&g_tc_error, 0u, 1u);
+}
+
 }  // namespace kgb
+
+extern "C" int kronmult_diag_wait_selftest(int *code)
+{
+    if (!code) return cudaErrorInvalidValue;
+    *code = 0;
+    const unsigned z = 0;
+    cudaError_t e = cudaMemcpyToSymbol(kgb::g_tc_error, &z, sizeof z);
+    if (e != cudaSuccess) return e;
+    kgb::wait_selftest_kernel<<<1, 32>>>();
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = cudaDeviceSynchronize()) != cudaSuccess) return e;
+    unsigned v = 0;
+    if ((e = cudaMemcpyFromSymbol(&v, kgb::g_tc_error, sizeof v)) != cudaSuccess) return e;
+    *code = (int)v;
+    return cudaMemcpyToSymbol(kgb::g_tc_error, &z, sizeof z);
+}
 
 extern "C" int kronmult_device_error(int *code, int clear)
 {

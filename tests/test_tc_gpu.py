@@ -93,3 +93,22 @@ def test_tc_rejects_unsupported_shape(cuda):
     b = W.make_batch(2, 4, 4, 2, 2, seed=1)
     with pytest.raises(K.KronmultError):
         run_mode(b, cuda, "tf32")
+
+
+def test_bounded_wait_runs_out_into_an_error_status(cuda):
+    """A wait on an mbarrier that nothing arrives on ends in the device error word
+    (code 1) instead of a hang; afterwards the context still runs the tensor-core
+    forward correctly and the error word is clear."""
+    import ctypes
+
+    from kronmult_gb300 import _lib
+
+    lib = _lib.lib()
+    code = ctypes.c_int(-1)
+    assert lib.kronmult_diag_wait_selftest(ctypes.byref(code)) == 0
+    assert code.value == 1
+    assert lib.kronmult_device_error(ctypes.byref(code), 0) == 0 and code.value == 0
+    from kronmult_gb300 import workloads as W
+
+    b = W.make_batch(3, 8, 8, 16, 4, seed=4242, factor_scale=1 / 8)
+    assert O.rel_l2(run_mode(b, cuda, "tf32"), O.forward(b)) <= TOL["tf32"]
