@@ -143,12 +143,15 @@ def cpu_baseline(b, dtype, budget_s: float = 15.0):
     from oracle import oracle as O
     from kronmult_gb300.workloads import Batch
 
-    threads = O.max_threads("port")
+    try:
+        threads = len(os.sched_getaffinity(0))
+    except AttributeError:
+        threads = os.cpu_count() or 1
     probe = min(b.nb, 2048)
     sub = Batch(b.name, b.d, b.n, b.stride, b.block, b.factors, b.inputs[:probe], b.out_init,
                 b.fac_index[:probe], b.out_index[:probe])
     t0 = time.perf_counter()
-    O.forward(sub, dtype=dtype)
+    O.forward(sub, dtype=dtype, nthreads=threads)
     t_probe = time.perf_counter() - t0
     per_entry = t_probe / probe
     count = int(min(b.nb, max(probe, budget_s / 3 / max(per_entry, 1e-12))))
@@ -157,7 +160,7 @@ def cpu_baseline(b, dtype, budget_s: float = 15.0):
     best = float("inf")
     for _ in range(3):
         t0 = time.perf_counter()
-        O.forward(sub, dtype=dtype)
+        O.forward(sub, dtype=dtype, nthreads=threads)
         best = min(best, time.perf_counter() - t0)
     flops = 2.0 * b.d * b.n * b.N * count
     return {"value": flops / best / 1e9, "unit": "GFLOP/s", "cores": threads, "kind": "port",
@@ -173,23 +176,28 @@ def run_reference(args, rank, world):
     from oracle import oracle as O
     from kronmult_gb300.workloads import Batch
 
-    threads = O.max_threads("port")
+    # every host core this process may run on (a launcher may have set OMP_NUM_THREADS=1
+    # for its ranks; the reference arm runs on rank 0 alone and uses them all)
+    try:
+        threads = len(os.sched_getaffinity(0))
+    except AttributeError:
+        threads = os.cpu_count() or 1
     # bounded sample per step so that warmup+steps stay within a few minutes
     probe = min(b.nb, 1024)
     sub = Batch(b.name, b.d, b.n, b.stride, b.block, b.factors, b.inputs[:probe], b.out_init,
                 b.fac_index[:probe], b.out_index[:probe])
     t0 = time.perf_counter()
-    O.forward(sub, dtype=dt)
+    O.forward(sub, dtype=dt, nthreads=threads)
     per_entry = (time.perf_counter() - t0) / probe
     total_steps = args.steps + args.warmup
     count = int(min(b.nb, max(64, 120.0 / total_steps / max(per_entry, 1e-12))))
     sub = Batch(b.name, b.d, b.n, b.stride, b.block, b.factors, b.inputs[:count], b.out_init,
                 b.fac_index[:count], b.out_index[:count])
     for _ in range(args.warmup):
-        O.forward(sub, dtype=dt)
+        O.forward(sub, dtype=dt, nthreads=threads)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        O.forward(sub, dtype=dt)
+        O.forward(sub, dtype=dt, nthreads=threads)
     el = time.perf_counter() - t0
     flops = 2.0 * b.d * b.n * b.N * count * args.steps
     v = flops / el / 1e9
