@@ -51,14 +51,26 @@ __device__ __forceinline__ uint32_t core_offset(uint32_t row, uint32_t kbyte)
     return (row >> 3) * 256u + (kbyte >> 4) * 128u + (row & 7u) * 16u + (kbyte & 15u);
 }
 
-__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr)
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo = 128u, uint32_t sbo = 256u)
 {
     uint64_t d = 0;
     d |= (uint64_t)((saddr >> 4) & 0x3FFFu);          // start address
-    d |= (uint64_t)((128u >> 4) & 0x3FFFu) << 16;     // leading byte offset (K direction)
-    d |= (uint64_t)((256u >> 4) & 0x3FFFu) << 32;     // stride byte offset (M/N direction)
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;      // leading byte offset (K direction)
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;      // stride byte offset (M/N direction)
     d |= (uint64_t)1u << 46;                          // descriptor version for sm_100 family
     return d;                                         // base offset 0, no swizzle
+}
+
+// The A operand (the vector: `tiles` tiles of 128 rows) uses the same core matrices
+// with a different arrangement: the k-chunk-0 core matrices of all rows first (8-row
+// groups 128 B apart, SBO = 128), the k-chunk-1 ones LBO = tiles*2048 + 64 bytes
+// later.  The two 16-byte halves of a row then sit 64 bytes apart modulo the 128-byte
+// bank row, so the epilogue's stores (consecutive lanes = consecutive rows, both
+// halves) and the staging conversion hit distinct banks.
+__device__ __forceinline__ uint32_t a_lbo(int tiles) { return (uint32_t)tiles * 2048u + 64u; }
+__device__ __forceinline__ uint32_t a_offset(uint32_t row, uint32_t kbyte, uint32_t lbo)
+{
+    return (row >> 3) * 128u + (kbyte >> 4) * lbo + (row & 7u) * 16u + (kbyte & 15u);
 }
 
 template <int KIND> __device__ __forceinline__ constexpr uint32_t instr_desc()
@@ -127,13 +139,17 @@ __device__ __forceinline__ float to_tf32(float x)
     return __uint_as_float(r);
 }
 
-// store one value of the operand element (row, k) in the operand type of KIND
-template <int KIND> __device__ __forceinline__ void put(unsigned char *base, uint32_t row, uint32_t k, float v)
+// store one value of the operand element (row, k) in the operand type of KIND: B
+// operands (factors) in the plain core-matrix layout, A (lbo != 0) in the split one
+template <int KIND>
+__device__ __forceinline__ void put(unsigned char *base, uint32_t row, uint32_t k, float v, uint32_t lbo = 0)
 {
+    constexpr uint32_t es = KIND == KIND_TF32 ? 4u : 2u;
+    const uint32_t off = lbo ? a_offset(row, k * es, lbo) : core_offset(row, k * es);
     if constexpr (KIND == KIND_TF32) {
-        *reinterpret_cast<float *>(base + core_offset(row, k * 4u)) = to_tf32(v);
+        *reinterpret_cast<float *>(base + off) = to_tf32(v);
     } else {
-        *reinterpret_cast<__nv_bfloat16 *>(base + core_offset(row, k * 2u)) = __float2bfloat16_rn(v);
+        *reinterpret_cast<__nv_bfloat16 *>(base + off) = __float2bfloat16_rn(v);
     }
 }
 
@@ -195,7 +211,7 @@ template <int KIND> __global__ void __launch_bounds__(kTcThreads, 4) fwd_tc_kern
     float *raw1 = fraw0 + d * 64;
     float *fraw1 = raw1 + N;
     unsigned char *xs = reinterpret_cast<unsigned char *>(fraw1 + d * 64);  // tiles x 4 KB
-    unsigned char *bs = xs + (size_t)a.tiles * kTileBytes;                  // d x 512 B
+    unsigned char *bs = xs + (size_t)a.tiles * kTileBytes + 64;             // d x 512 B
     uint64_t *mbar = reinterpret_cast<uint64_t *>(bs + (size_t)d * kBBytes);
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -205,7 +221,7 @@ template <int KIND> __global__ void __launch_bounds__(kTcThreads, 4) fwd_tc_kern
     if (e >= e_end) return;
 
     // operands zeroed once: padding rows of B (8..15) and, for BF16, the K 8..15 half of A stay zero
-    for (int v = tid; v < (a.tiles * kTileBytes + d * kBBytes) / 16; v += kTcThreads)
+    for (int v = tid; v < (a.tiles * kTileBytes + 64 + d * kBBytes) / 16; v += kTcThreads)
         reinterpret_cast<int4 *>(xs)[v] = make_int4(0, 0, 0, 0);
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
@@ -228,6 +244,7 @@ template <int KIND> __global__ void __launch_bounds__(kTcThreads, 4) fwd_tc_kern
     const uint32_t tacc = tmem + 16u * a.tiles;  // run accumulator: one 16-column block per tile
     const uint32_t mbar_a = smem_u32(mbar);
     const uint32_t xs_a = smem_u32(xs), bs_a = smem_u32(bs);
+    const uint32_t lboa = a_lbo(a.tiles);  // A operand: k-chunk-1 core matrices this far after chunk 0
     uint32_t phase = 0;
     bool failed = false;
     double *cur = nullptr;
@@ -266,10 +283,10 @@ template <int KIND> __global__ void __launch_bounds__(kTcThreads, 4) fwd_tc_kern
         for (int q = tid; q < N / 4; q += kTcThreads) {
             const float4 v4 = *reinterpret_cast<const float4 *>(raw + 4 * q);
             const uint32_t c = q >> 1, k0 = (q & 1) * 4;
-            put<KIND>(xs, c, k0 + 0, v4.x);
-            put<KIND>(xs, c, k0 + 1, v4.y);
-            put<KIND>(xs, c, k0 + 2, v4.z);
-            put<KIND>(xs, c, k0 + 3, v4.w);
+            put<KIND>(xs, c, k0 + 0, v4.x, lboa);
+            put<KIND>(xs, c, k0 + 1, v4.y, lboa);
+            put<KIND>(xs, c, k0 + 2, v4.z, lboa);
+            put<KIND>(xs, c, k0 + 3, v4.w, lboa);
         }
         // the run continues when this entry adds into the same output as the previous one;
         // otherwise the previous run's sum leaves TMEM before the last mode overwrites it
@@ -286,7 +303,7 @@ template <int KIND> __global__ void __launch_bounds__(kTcThreads, 4) fwd_tc_kern
                 const uint32_t dst = i > 0 ? tmem : tacc;
                 const uint32_t accumulate = (i == 0 && cont) ? 1u : 0u;
                 for (int t = 0; t < a.tiles; ++t)
-                    mma<KIND>(dst + 16u * t, smem_desc(xs_a + t * kTileBytes), smem_desc(bs_a + i * kBBytes),
+                    mma<KIND>(dst + 16u * t, smem_desc(xs_a + t * 2048u, lboa, 128u), smem_desc(bs_a + i * kBBytes),
                               accumulate);
                 mma_commit(mbar_a);
             }
@@ -314,7 +331,7 @@ template <int KIND> __global__ void __launch_bounds__(kTcThreads, 4) fwd_tc_kern
 #pragma unroll
                         for (int r = 0; r < 8; ++r) {
                             const uint32_t p = c + r * F;
-                            put<KIND>(xs, p >> 3, p & 7, v[t][r]);
+                            put<KIND>(xs, p >> 3, p & 7, v[t][r], lboa);
                         }
                     }
                 }
@@ -358,7 +375,7 @@ int launch_tc_forward(int kind, int d, int n, const float *const *mats, int stri
     int cols = 32;
     while (cols < 2 * 16 * a.tiles) cols *= 2;  // mode output + run accumulator
     a.tmem_cols = cols;
-    const size_t need = (size_t)2 * (a.N + d * 64) * sizeof(float) + (size_t)a.tiles * kTileBytes +
+    const size_t need = (size_t)2 * (a.N + d * 64) * sizeof(float) + (size_t)a.tiles * kTileBytes + 64 +
                         (size_t)d * kBBytes + 16;
     // resident CTAs per SM are limited so that their tensor-memory columns fit in 512:
     // each CTA reserves 1/max_ctas of the SM's shared memory (less the per-CTA system
