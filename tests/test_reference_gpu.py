@@ -88,3 +88,29 @@ def test_shared_outputs_vs_reference_kernel(cuda, cfg):
     db.forward(sync=True)
     err = (torch.linalg.norm(db.outputs - want) / torch.linalg.norm(want)).item()
     assert err <= 1e-13
+
+
+@pytest.mark.parametrize("seed", list(range(16)))
+def test_bitwise_random_shapes(cuda, seed):
+    """Seeded random shapes (n = 1..10, strides beyond n, one output per entry): our
+    forward and the reference kernel agree bit for bit in FP64, and in FP32 where the
+    reference float kernel is well defined (N <= 1024 or a multiple of 1024)."""
+    needs_ref()
+    from kronmult_gb300 import DeviceBatch
+    from kronmult_gb300 import workloads as W
+
+    rng = np.random.Generator(np.random.PCG64(9100 + seed))
+    n = int(rng.integers(1, 11))
+    max_d = max(1, int(np.floor(np.log(20000) / np.log(max(n, 2)))))
+    d = int(rng.integers(1, min(max_d, 7) + 1))
+    stride = n + int(rng.integers(0, 3))
+    nb = int(rng.integers(1, 40))
+    b = W.make_batch(d, n, stride, nb, 1, seed=9200 + seed)
+    for dtype, tag in ((torch.float64, "f64"), (torch.float32, "f32")):
+        N = n ** d
+        if tag == "f32" and N > 1024 and N % 1024:
+            continue
+        db = DeviceBatch.from_host(b, device=cuda, dtype=dtype, with_workspace=True)
+        want = reference_run(db, tag)
+        db.forward(sync=True)
+        assert torch.equal(db.outputs, want), (d, n, stride, nb, tag)
