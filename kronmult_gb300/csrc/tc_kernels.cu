@@ -181,14 +181,29 @@ __device__ __forceinline__ void tc_load_ptrs(TcPtrs &p, const TcArgs &a, long lo
 }
 
 // asynchronous copy of one entry into a raw staging slot: the vector in natural
-// order, the factors as fraw[i*64 + r + 8k] = A_i(r, k)
-__device__ __forceinline__ void tc_stage_async(float *raw, float *fraw, const TcPtrs &p, const TcArgs &a, int tid)
+// order, the factors as fraw[i*64 + r + 8k] = A_i(r, k).  The vector is one TMA bulk
+// copy (cp.async.bulk) issued by thread 0 and completed on the staging barrier `sbar`
+// when its source is 16-byte aligned; otherwise every thread copies 4-byte elements
+// with cp.async and thread 0 completes the barrier's phase without bytes.  Either way
+// the staging barrier completes exactly one phase per entry.
+__device__ __forceinline__ void tc_stage_async(float *raw, float *fraw, const TcPtrs &p, const TcArgs &a, int tid,
+                                               uint32_t sbar)
 {
     const int N = a.N;
-    if (((reinterpret_cast<uintptr_t>(p.src) & 15u) == 0) && ((N & 3) == 0)) {
-        for (int q = tid; q < N / 4; q += kTcThreads) cp_async<16>(raw + 4 * q, p.src + 4 * q);
+    const unsigned bytes = (unsigned)N * 4u;
+    if (((reinterpret_cast<uintptr_t>(p.src) & 15u) == 0) && ((bytes & 15u) == 0)) {
+        if (tid == 0) {
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(sbar), "r"(bytes)
+                         : "memory");
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                    smem_u32(raw)),
+                "l"(p.src), "r"(bytes), "r"(sbar)
+                : "memory");
+        }
     } else {
         for (int q = tid; q < N; q += kTcThreads) cp_async<4>(raw + q, p.src + q);
+        if (tid == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(sbar) : "memory");
     }
 #pragma unroll
     for (int s = 0; s < kTcFacSlots; ++s) {
@@ -212,8 +227,9 @@ template <int KIND> __global__ void __launch_bounds__(kTcThreads, 4) fwd_tc_kern
     float *fraw1 = raw1 + N;
     unsigned char *xs = reinterpret_cast<unsigned char *>(fraw1 + d * 64);  // tiles x 4 KB
     unsigned char *bs = xs + (size_t)a.tiles * kTileBytes + 64;             // d x 512 B
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(bs + (size_t)d * kBBytes);
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 1);
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(bs + (size_t)d * kBBytes);  // MMA completion
+    uint64_t *sbar = mbar + 1;                                                  // staging completion
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 2);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     long long e = (long long)blockIdx.x * a.entries_per_cta;
@@ -229,13 +245,15 @@ template <int KIND> __global__ void __launch_bounds__(kTcThreads, 4) fwd_tc_kern
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
+    const uint32_t sbar_a = smem_u32(sbar);
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sbar_a) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     TcPtrs nxt;
     tc_load_ptrs(nxt, a, e, tid);
-    tc_stage_async(raw0, fraw0, nxt, a, tid);
+    tc_stage_async(raw0, fraw0, nxt, a, tid, sbar_a);
     if (e + 1 < e_end) tc_load_ptrs(nxt, a, e + 1, tid);
     tc_fence_before();
     __syncthreads();
@@ -245,8 +263,9 @@ template <int KIND> __global__ void __launch_bounds__(kTcThreads, 4) fwd_tc_kern
     const uint32_t mbar_a = smem_u32(mbar);
     const uint32_t xs_a = smem_u32(xs), bs_a = smem_u32(bs);
     const uint32_t lboa = a_lbo(a.tiles);  // A operand: k-chunk-1 core matrices this far after chunk 0
-    uint32_t phase = 0;
+    uint32_t phase = 0, sphase = 0;
     bool failed = false;
+    bool staging = true;  // a staging copy is in flight whose phase has not been waited for
     double *cur = nullptr;
     constexpr int MAXT = 4;  // tiles per entry (N <= 4096)
 
@@ -270,9 +289,17 @@ template <int KIND> __global__ void __launch_bounds__(kTcThreads, 4) fwd_tc_kern
         float *raw = slot ? raw1 : raw0, *fraw = slot ? fraw1 : fraw0;
         double *o = a.out[e];
         cp_async_wait_all();
-        __syncthreads();  // slot complete for every thread; the previous entry's MMAs are done
+        const bool staged = mbar_wait(sbar_a, sphase);  // the slot's bulk copy (or its empty phase)
+        if (__syncthreads_or(!staged)) {  // slot complete for every thread; previous MMAs done
+            if (tid == 0) atomicCAS(&g_tc_error, 0u, 1u);
+            failed = true;
+            break;
+        }
+        sphase ^= 1u;
+        staging = false;
         if (e + 1 < e_end) {
-            tc_stage_async(slot ? raw0 : raw1, slot ? fraw0 : fraw1, nxt, a, tid);
+            tc_stage_async(slot ? raw0 : raw1, slot ? fraw0 : fraw1, nxt, a, tid, sbar_a);
+            staging = true;
             if (e + 2 < e_end) tc_load_ptrs(nxt, a, e + 2, tid);
         }
         // operands: B_i[row r][k] = A_i(r, k); input natural index p = k + 8c -> A row c, column k
@@ -343,6 +370,9 @@ template <int KIND> __global__ void __launch_bounds__(kTcThreads, 4) fwd_tc_kern
         if (failed) break;
     }
     cp_async_wait_all();
+    // leaving early with a bulk copy still in flight: one more bounded wait for it, so
+    // that it does not land in shared memory after this CTA is gone
+    if (failed && staging) mbar_wait(sbar_a, sphase);
     if (cur != nullptr && !failed) flush(cur);
     tc_fence_before();
     __syncthreads();
@@ -376,7 +406,7 @@ int launch_tc_forward(int kind, int d, int n, const float *const *mats, int stri
     while (cols < 2 * 16 * a.tiles) cols *= 2;  // mode output + run accumulator
     a.tmem_cols = cols;
     const size_t need = (size_t)2 * (a.N + d * 64) * sizeof(float) + (size_t)a.tiles * kTileBytes + 64 +
-                        (size_t)d * kBBytes + 16;
+                        (size_t)d * kBBytes + 32;  // + two mbarriers and the TMEM address
     // resident CTAs per SM are limited so that their tensor-memory columns fit in 512:
     // each CTA reserves 1/max_ctas of the SM's shared memory (less the per-CTA system
     // reservation), so exactly max_ctas fit

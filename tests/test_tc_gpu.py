@@ -112,3 +112,27 @@ def test_bounded_wait_runs_out_into_an_error_status(cuda):
 
     b = W.make_batch(3, 8, 8, 16, 4, seed=4242, factor_scale=1 / 8)
     assert O.rel_l2(run_mode(b, cuda, "tf32"), O.forward(b)) <= TOL["tf32"]
+
+
+@pytest.mark.parametrize("compute", ["tf32", "bf16"])
+def test_tc_unaligned_inputs(cuda, compute):
+    """Input vectors that do not start on a 16-byte boundary take the element-wise
+    staging path (no bulk copy); results as with aligned inputs."""
+    import ctypes
+
+    from kronmult_gb300 import DeviceBatch, _lib
+    from kronmult_gb300 import workloads as W
+
+    b = W.make_batch(3, 8, 8, 6, 3, seed=4343, factor_scale=1 / 8)
+    db = DeviceBatch.from_host(b, device=cuda, dtype=torch.float32, out_dtype=torch.float64)
+    shifted = torch.zeros((b.nb, b.N + 1), dtype=torch.float32, device=cuda)
+    shifted[:, 1:] = db.inputs
+    k = torch.arange(b.nb, device=cuda, dtype=torch.int64)
+    in_ptrs = (shifted.data_ptr() + 4 + k * ((b.N + 1) * 4)).contiguous()
+    code = {"tf32": _lib.KRONMULT_COMPUTE_TF32, "bf16": _lib.KRONMULT_COMPUTE_BF16}[compute]
+    st = _lib.lib().kronmult_batched_f32_f64out_async(b.d, b.n, db.mat_ptrs.data_ptr(), b.stride, in_ptrs.data_ptr(),
+                                                      db.out_ptrs.data_ptr(), None, b.nb, code, None, None)
+    assert st == 0
+    torch.cuda.synchronize()
+    assert ctypes_device_error() == 0
+    assert O.rel_l2(db.outputs.cpu().numpy(), O.forward(b)) <= TOL[compute]
