@@ -615,7 +615,7 @@ def main():
         forward_from_host(db, h_in, h_fac, h_out, chunks=12, streams=pipe_streams)
 
     def e2e_mapped_step():
-        # kernels read inputs and factors from pinned host memory; outputs copied back in 2 pieces
+        # kernels read inputs and factors from pinned host memory; outputs copied back in 2 pieces (9:1)
         forward_from_host_mapped(db, h_in, h_fac, h_out, chunks=2, streams=pipe_streams)
 
     def time_host_steps(step):

@@ -265,13 +265,16 @@ def host_device_pointer(t: torch.Tensor) -> int:
 
 
 def forward_from_host_mapped(b: DeviceBatch, h_inputs: torch.Tensor, h_factors: torch.Tensor,
-                             h_outputs: torch.Tensor, chunks: int = 2, streams=None):
+                             h_outputs: torch.Tensor, chunks: int = 2, streams=None, last_share: float = 0.1):
     """End-to-end forward whose kernels read the inputs and factors straight from pinned
     host memory over the CPU-GPU link (no staging copy); the outputs are accumulated in
     device memory and copied back piecewise, the copy of piece i overlapping the
     forward of piece i+1.  On GB300 the copy engines move about 0.2 TB/s host-to-device
     (the FP64 forward alone streams its inputs at that rate), while the SMs read the
-    inputs over the link with the forward slowed by under 2 %.  `h_inputs` and
+    inputs over the link with the forward slowed by under 2 %.  Only the last piece's
+    copy back is exposed, so the last piece takes `last_share` of the output groups
+    (the others share the rest evenly): on the 36864-entry FP64 batch two pieces split
+    9:1 measured 6.74 ms against 6.89 ms for an even split.  `h_inputs` and
     `h_factors` must be contiguous pinned tensors shaped like the batch's inputs and
     factors.  Enqueues only; synchronise with torch.cuda.synchronize()."""
     for h, t in ((h_inputs, b.inputs), (h_factors, b.factors)):
@@ -292,7 +295,7 @@ def forward_from_host_mapped(b: DeviceBatch, h_inputs: torch.Tensor, h_factors: 
         cache.clear()
         cache[key] = (in_ptrs, mat_ptrs)
     in_ptrs, mat_ptrs = cache[key]
-    cuts, _, out_rows, _, out_monotone = _host_pipeline_plan(b, chunks)
+    cuts, _, out_rows, _, out_monotone = _host_pipeline_plan(b, chunks, last_share)
     nchunks = len(cuts) - 1
     es_p = 8
     fn = getattr(_lib.lib(), _FN[b.inputs.dtype] + "_async")
@@ -317,21 +320,31 @@ def forward_from_host_mapped(b: DeviceBatch, h_inputs: torch.Tensor, h_factors: 
     return s_cmp, s_out
 
 
-def _host_pipeline_plan(b: DeviceBatch, chunks: int):
+def _host_pipeline_plan(b: DeviceBatch, chunks: int, last_share: float | None = None):
     """Piece boundaries of forward_from_host (cut at output-group starts), the factor
     rows and output rows each piece touches, and whether factor sets and outputs are
-    used in increasing order.  Computed once per batch and piece count from host
-    copies of the index maps, so repeated calls make no device-to-host transfer."""
+    used in increasing order.  Pieces hold equal numbers of output groups, or, with
+    `last_share` in (0, 1) and more than one piece, the last piece holds that share of
+    the groups and the others split the rest evenly.  Computed once per batch and
+    piece layout from host copies of the index maps, so repeated calls make no
+    device-to-host transfer."""
+    if last_share is not None and not 0.0 < last_share < 1.0:
+        raise ValueError("last_share must lie in (0, 1)")
+    key = (chunks, last_share)
     cache = b.__dict__.setdefault("_host_plans", {})
-    if chunks in cache:
-        return cache[chunks]
+    if key in cache:
+        return cache[key]
     nb = b.nb
     oi = b.out_index.cpu()
     fi = b.fac_index.cpu()
     starts = torch.nonzero(torch.cat([torch.tensor([True]), oi[1:] != oi[:-1]])).flatten().tolist() + [nb]
     ngroups = len(starts) - 1
     chunks = max(1, min(chunks, ngroups))
-    cuts = [starts[(ngroups * c) // chunks] for c in range(chunks)] + [nb]
+    if last_share is None or chunks == 1:
+        cuts = [starts[(ngroups * c) // chunks] for c in range(chunks)] + [nb]
+    else:
+        head = min(ngroups - 1, max(chunks - 1, int(round(ngroups * (1.0 - last_share)))))
+        cuts = [starts[(head * c) // (chunks - 1)] for c in range(chunks - 1)] + [starts[head], nb]
     monotone = bool(torch.all(fi[1:] >= fi[:-1])) if nb > 1 else True
     out_monotone = bool(torch.all(oi[1:] >= oi[:-1])) if nb > 1 else True
     fac_rows, out_rows = [], []
@@ -344,7 +357,7 @@ def _host_pipeline_plan(b: DeviceBatch, chunks: int):
             fac_rows.append((0, 0))
             out_rows.append((0, 0))
     plan = (cuts, fac_rows, out_rows, monotone, out_monotone)
-    cache[chunks] = plan
+    cache[key] = plan
     return plan
 
 

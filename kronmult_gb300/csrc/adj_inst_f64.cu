@@ -1,6 +1,6 @@
 // Explicit instantiation of the adjoint kernels for double.
 #include "adj_kernels.cuh"
-KGB_ADJ_INSTANTIATE(double)
+KGB_ADJ_INSTANTIATE_NN(double)
 
 namespace kgb {
 // the FP64 adjoint always uses the element-mapped kernel

@@ -50,29 +50,41 @@ template <typename T> struct AdjArgs {
 // fibre mapping would leave 28 of 32 lanes idle in every second pass, and the FP64
 // pipe is charged per warp instruction.
 
+// NN > 0: n known at compile time (index arithmetic and k-loops resolved, fibres read
+// with their widest aligned loads); NN = 0: n = the run-time argument.
+
 // forward-style mode product (contract the fastest index), src -> dst:
 // dst[c + r*F] = sum_k A(r, k) src[k + c*n]
-template <typename T>
-__device__ __forceinline__ void mode_fast_elem(const T *__restrict__ src, T *__restrict__ dst, const T *M, int n,
+template <typename T, int NN>
+__device__ __forceinline__ void mode_fast_elem(const T *__restrict__ src, T *__restrict__ dst, const T *M, int n_rt,
                                                int N, const Team &tm)
 {
+    const int n = NN ? NN : n_rt;
     const int F = N / n;
     for (int q = tm.rank; q < N; q += tm.size) {
         // row r = q % n of fibre c = q / n: lanes of one fibre read the same words
         const int c = q / n, r = q - c * n;
         const T *x = src + c * n;
         T s = T(0);
+        if constexpr (NN > 0) {
+            T xv[NN];
+            load_fibre<T, NN>(x, xv);
+#pragma unroll
+            for (int k = 0; k < NN; ++k) s = fma_t<T>(M[r + k * NN], xv[k], s);
+        } else {
 #pragma unroll 8
-        for (int k = 0; k < n; ++k) s = fma_t<T>(M[r + k * n], x[k], s);
+            for (int k = 0; k < n; ++k) s = fma_t<T>(M[r + k * n], x[k], s);
+        }
         dst[c + r * F] = s;
     }
 }
 
 // transposed mode product contracting the slowest index, in place through registers:
 // Z[r + n*t] = sum_k A(k, r) Q[t + R*k]
-template <typename T, int EMAX>
-__device__ __forceinline__ void mode_slow_elem(T *buf, const T *M, int n, int N, const Team &tm)
+template <typename T, int NN, int EMAX>
+__device__ __forceinline__ void mode_slow_elem(T *buf, const T *M, int n_rt, int N, const Team &tm)
 {
+    const int n = NN ? NN : n_rt;
     const int R = N / n;
     T z[EMAX];
 #pragma unroll
@@ -95,12 +107,12 @@ __device__ __forceinline__ void mode_slow_elem(T *buf, const T *M, int n, int N,
     tm.sync();
 }
 
-template <typename T, int EMAX>
+template <typename T, int NN, int EMAX>
 __global__ void __launch_bounds__(512) adj_elem_kernel(const AdjArgs<T> a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const Team tm(a.team_size);
-    const int n = a.n, N = a.N, d = a.d, R = N / n, P = n * n;
+    const int n = NN ? NN : a.n, N = a.N, d = a.d, R = N / n, P = n * n;
     T *base = reinterpret_cast<T *>(smem_raw) + (size_t)tm.id * a.team_elems;
     // slice layout: [p buffers][q][fac d*P][gacc d*P][gpart slices*P][cur grad pointers d]
     const int np = a.store_all ? d : 3;
@@ -156,7 +168,7 @@ __global__ void __launch_bounds__(512) adj_elem_kernel(const AdjArgs<T> a)
         tm.sync();
         if (a.store_all) {
             for (int i = d - 1; i >= 1; --i) {
-                mode_fast_elem<T>(pb + (size_t)i * a.npad, pb + (size_t)(i - 1) * a.npad, fac + i * P, n, N, tm);
+                mode_fast_elem<T, NN>(pb + (size_t)i * a.npad, pb + (size_t)(i - 1) * a.npad, fac + i * P, n, N, tm);
                 tm.sync();
             }
         }
@@ -170,7 +182,7 @@ __global__ void __launch_bounds__(512) adj_elem_kernel(const AdjArgs<T> a)
                     const T *src = pb;
                     T *dst = pb + a.npad;
                     for (int m = d - 1; m > i; --m) {
-                        mode_fast_elem<T>(src, dst, fac + m * P, n, N, tm);
+                        mode_fast_elem<T, NN>(src, dst, fac + m * P, n, N, tm);
                         tm.sync();
                         src = dst;
                         dst = (dst == pb + a.npad) ? pb + 2 * (size_t)a.npad : pb + a.npad;
@@ -195,7 +207,7 @@ __global__ void __launch_bounds__(512) adj_elem_kernel(const AdjArgs<T> a)
                     gacc[i * P + pr] += s;
                 }
             }
-            if (i < d - 1 || want_gin) mode_slow_elem<T, EMAX>(qb, fac + i * P, n, N, tm);
+            if (i < d - 1 || want_gin) mode_slow_elem<T, NN, EMAX>(qb, fac + i * P, n, N, tm);
         }
         if (want_gin) {
             T *gi = a.gin[e];
@@ -403,21 +415,45 @@ __global__ void __launch_bounds__(256, 3) adj_smem_kernel(const AdjArgs<T> a)
 }
 
 template <typename T> using AdjFn = void (*)(const AdjArgs<T>);
-template <typename T> AdjFn<T> adj_lookup(int emax);
+template <typename T> AdjFn<T> adj_lookup(int nn, int emax);
 template <typename T> AdjFn<T> adj_fibre_lookup(int nn, int qmax);
 
 }  // namespace kgb
 
+// element-mapped kernels of one n (0 = run-time n), lookup key n * 32 + EMAX
+#define KGB_ADJ_ELEM_CASES(T, NN)                                                                      \
+    case NN * 32 + 1: return adj_elem_kernel<T, NN, 1>;                                                \
+    case NN * 32 + 2: return adj_elem_kernel<T, NN, 2>;                                                \
+    case NN * 32 + 4: return adj_elem_kernel<T, NN, 4>;                                                \
+    case NN * 32 + 8: return adj_elem_kernel<T, NN, 8>;                                                \
+    case NN * 32 + 16: return adj_elem_kernel<T, NN, 16>;
+
+// run-time n only (nn is ignored)
 #define KGB_ADJ_INSTANTIATE(T)                                                                         \
     namespace kgb {                                                                                    \
-    template <> AdjFn<T> adj_lookup<T>(int emax)                                                       \
+    template <> AdjFn<T> adj_lookup<T>(int, int emax)                                                  \
     {                                                                                                  \
         switch (emax) {                                                                                \
-        case 1: return adj_elem_kernel<T, 1>;                                                          \
-        case 2: return adj_elem_kernel<T, 2>;                                                          \
-        case 4: return adj_elem_kernel<T, 4>;                                                          \
-        case 8: return adj_elem_kernel<T, 8>;                                                          \
-        case 16: return adj_elem_kernel<T, 16>;                                                        \
+            KGB_ADJ_ELEM_CASES(T, 0)                                                                   \
+        default: return nullptr;                                                                       \
+        }                                                                                              \
+    }                                                                                                  \
+    }
+
+// compile-time n for 2 <= n <= 8, run-time n otherwise
+#define KGB_ADJ_INSTANTIATE_NN(T)                                                                      \
+    namespace kgb {                                                                                    \
+    template <> AdjFn<T> adj_lookup<T>(int nn, int emax)                                               \
+    {                                                                                                  \
+        switch ((nn >= 2 && nn <= 8 ? nn : 0) * 32 + emax) {                                           \
+            KGB_ADJ_ELEM_CASES(T, 0)                                                                   \
+            KGB_ADJ_ELEM_CASES(T, 2)                                                                   \
+            KGB_ADJ_ELEM_CASES(T, 3)                                                                   \
+            KGB_ADJ_ELEM_CASES(T, 4)                                                                   \
+            KGB_ADJ_ELEM_CASES(T, 5)                                                                   \
+            KGB_ADJ_ELEM_CASES(T, 6)                                                                   \
+            KGB_ADJ_ELEM_CASES(T, 7)                                                                   \
+            KGB_ADJ_ELEM_CASES(T, 8)                                                                   \
         default: return nullptr;                                                                       \
         }                                                                                              \
     }                                                                                                  \

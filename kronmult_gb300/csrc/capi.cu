@@ -132,16 +132,22 @@ static int adjoint_async(int d, int n, const T *const *mats, int stride, const T
         int emax = 1;
         while (emax < per) emax *= 2;
         if (emax > 16) return cudaErrorNotSupported;
-        fn = adj_lookup<T>(emax);
+        fn = adj_lookup<T>(n, emax);
         if (!fn) return cudaErrorNotSupported;
-        // gradient contraction items (pair, slice): slices * P a multiple of the team size
-        int g = P, h = ts;
-        while (h) {
-            const int t = g % h;
-            g = h;
-            h = t;
+        // gradient contraction items (pair, slice of t): S slices cost about
+        // ceil(S*P / lanes) passes of ceil(R / S) FMAs plus ceil(P / lanes) passes of S
+        // additions to sum the slices (lanes = min(team, 32): the FP64 pipe is charged per
+        // warp instruction); take the cheapest S, the smallest among equals
+        const int lanes = ts < 32 ? ts : 32;
+        long long best = -1;
+        for (int S = 1; S <= R && S <= 64; ++S) {
+            const long long cost = (long long)((S * P + lanes - 1) / lanes) * ((R + S - 1) / S) +
+                                   (long long)((P + lanes - 1) / lanes) * S;
+            if (best < 0 || cost < best) {
+                best = cost;
+                slices = S;
+            }
         }
-        slices = ts / g;
     }
     if (slices < 1) slices = 1;
     if (slices > R) slices = R;

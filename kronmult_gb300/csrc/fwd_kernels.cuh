@@ -810,13 +810,15 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) fwd_single_kernel
     }
 }
 
-// One entry per team with output elements (not whole fibres) mapped to threads,
-// runtime n: every lane has work for any n.  Selected for FP64 with odd n when the
-// fibre mapping would leave more than a tenth of the lanes idle (for example n = 7,
-// d = 3: 49 fibres per mode on 16-lane teams), since the FP64 pipe is charged per
+// The element mapping with n known at compile time: each thread owns up to EMAX
+// output elements of every mode (consecutive lanes take consecutive rows of one
+// fibre, which they read with the fibre's widest aligned loads as a broadcast), so
+// the team's lanes stay busy whatever F is, while the index arithmetic and the
+// k-loop are resolved at compile time.  Same k-ascending FMA chain per element as the
+// fibre kernels (bitwise the same values).  FP64 only: there the pipe is charged per
 // warp instruction whatever the number of active lanes.
-template <typename T, typename TO, int EMAX>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) fwd_single_elem_kernel(const FwdArgs<T, TO> a)
+template <typename T, typename TO, int NN, int EMAX>
+__global__ void __launch_bounds__(256, 3) fwd_single_elem_kernel(const FwdArgs<T, TO> a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const Team tm(a.team_size);
@@ -824,28 +826,24 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) fwd_single_elem_k
     T *fac = buf + a.vec_pad;
     const long long e = (long long)blockIdx.x * a.teams_per_cta + tm.id;
     if (e >= a.nb) return;
-    const int n = a.n, N = a.N, F = N / n, P = n * n;
+    const int N = a.N, F = N / NN;
+    constexpr int P = NN * NN;
     stage_vector(buf, a.in[e], N, tm);
-    {
-        const T *const *mats = a.mats + e * a.d;
-        for (int idx = tm.rank; idx < a.d * P; idx += tm.size) {
-            const int i = idx / P, rem = idx - i * P, k = rem / n, r = rem - k * n;
-            fac[idx] = mats[i][r + (size_t)k * a.stride];
-        }
-    }
+    stage_factors<T, NN>(fac, a.mats + e * a.d, a.d, a.stride, tm);
     tm.sync();
     T y[EMAX];
     for (int i = a.d - 1; i >= 0; --i) {
         const T *M = fac + i * P;
 #pragma unroll
         for (int j = 0; j < EMAX; ++j) {
-            const int q = tm.rank + j * tm.size;  // row r = q % n of fibre c = q / n
+            const int q = tm.rank + j * tm.size;  // row r = q % NN of fibre c = q / NN
             if (q < N) {
-                const int c = q / n, r = q - c * n;
-                const T *x = buf + c * n;
+                const int c = q / NN, r = q - c * NN;
+                T x[NN];
+                load_fibre<T, NN>(buf + c * NN, x);
                 T s = T(0);
-#pragma unroll 8
-                for (int k = 0; k < n; ++k) s = fma_t<T>(M[r + k * n], x[k], s);
+#pragma unroll
+                for (int k = 0; k < NN; ++k) s = fma_t<T>(M[r + k * NN], x[k], s);
                 y[j] = s;
             }
         }
@@ -855,7 +853,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) fwd_single_elem_k
             for (int j = 0; j < EMAX; ++j) {
                 const int q = tm.rank + j * tm.size;
                 if (q < N) {
-                    const int c = q / n, r = q - c * n;
+                    const int c = q / NN, r = q - c * NN;
                     buf[c + r * F] = y[j];
                 }
             }
@@ -867,7 +865,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) fwd_single_elem_k
     for (int j = 0; j < EMAX; ++j) {
         const int q = tm.rank + j * tm.size;
         if (q < N) {
-            const int c = q / n, r = q - c * n;
+            const int c = q / NN, r = q - c * NN;
             atomic_add<TO>(o + c + r * F, (TO)y[j]);
         }
     }
@@ -995,13 +993,20 @@ __global__ void __launch_bounds__(256) fwd_generic_kernel(const FwdArgs<T, TO> a
 template <typename T, typename TO> using FwdSmemFn = void (*)(const FwdArgs<T, TO>);
 template <typename T, typename TO> FwdSmemFn<T, TO> fwd_smem_lookup(int nn, int qmax);
 template <typename T, typename TO> FwdSmemFn<T, TO> fwd_single_lookup(int nn, int qmax);
-template <typename T, typename TO> FwdSmemFn<T, TO> fwd_single_elem_lookup(int emax);
+template <typename T, typename TO> FwdSmemFn<T, TO> fwd_single_elem_lookup(int nn, int emax);
 template <typename T, typename TO> FwdSmemFn<T, TO> fwd_global_lookup(int nn);
 template <typename T, typename TO> FwdSmemFn<T, TO> split_pass1_lookup(int nn, int qmax);
 template <typename T, typename TO> FwdSmemFn<T, TO> split_pass2_lookup(int nn);
 template <typename T, typename TO> void *fwd_generic_ptr();
 
 }  // namespace kgb
+
+// the element-mapped kernels of one n (lookup key n * 32 + EMAX)
+#define KGB_ELEM_CASES(T, TO, NN)                                                                     \
+    case NN * 32 + 1: return fwd_single_elem_kernel<T, TO, NN, 1>;                                    \
+    case NN * 32 + 2: return fwd_single_elem_kernel<T, TO, NN, 2>;                                    \
+    case NN * 32 + 4: return fwd_single_elem_kernel<T, TO, NN, 4>;                                    \
+    case NN * 32 + 8: return fwd_single_elem_kernel<T, TO, NN, 8>;
 
 // explicit instantiation of the forward kernels for one (T, TO) pair
 #define KGB_FWD_INSTANTIATE(T, TO)                                                                     \
@@ -1066,15 +1071,21 @@ template <typename T, typename TO> void *fwd_generic_ptr();
         default: return nullptr;                                                                       \
         }                                                                                              \
     }                                                                                                  \
-    template <> FwdSmemFn<T, TO> fwd_single_elem_lookup<T, TO>(int emax)                              \
+    template <> FwdSmemFn<T, TO> fwd_single_elem_lookup<T, TO>(int nn, int emax)                       \
     {                                                                                                  \
-        switch (emax) {                                                                                \
-        case 1: return fwd_single_elem_kernel<T, TO, 1>;                                               \
-        case 2: return fwd_single_elem_kernel<T, TO, 2>;                                               \
-        case 4: return fwd_single_elem_kernel<T, TO, 4>;                                               \
-        case 8: return fwd_single_elem_kernel<T, TO, 8>;                                               \
-        case 16: return fwd_single_elem_kernel<T, TO, 16>;                                             \
-        default: return nullptr;                                                                       \
+        if constexpr (sizeof(T) == 8) {                                                                \
+            switch (nn * 32 + emax) {                                                                  \
+                KGB_ELEM_CASES(T, TO, 2)                                                              \
+                KGB_ELEM_CASES(T, TO, 3)                                                              \
+                KGB_ELEM_CASES(T, TO, 4)                                                              \
+                KGB_ELEM_CASES(T, TO, 5)                                                              \
+                KGB_ELEM_CASES(T, TO, 6)                                                              \
+                KGB_ELEM_CASES(T, TO, 7)                                                              \
+                KGB_ELEM_CASES(T, TO, 8)                                                              \
+            default: return nullptr;                                                                   \
+            }                                                                                          \
+        } else {                                                                                       \
+            return nullptr;                                                                            \
         }                                                                                              \
     }                                                                                                  \
     template <> FwdSmemFn<T, TO> fwd_global_lookup<T, TO>(int nn)                                     \

@@ -249,24 +249,31 @@ int plan_forward(FwdPlan<T, TO> &pl, int d, int n, const T *const *mats, int str
             const int team_elems = vpad + fpad;
             int teams = 256 / ts;
             auto fn = fwd_single_lookup<T, TO>(n, qmax);
-            // whole fibres per thread leave (ts*qmax - F) of ts*qmax slots idle; when that
-            // is more than a tenth, map output elements to threads instead -- FP64 with
-            // odd n only (n = 3, 5, 7: fibres of 8-byte loads).  For FP32, and for FP64
-            // fibres of 16-byte loads (n = 6: measured up to 34 % faster than elements),
-            // the fibre's register reuse is worth more.
+            // Whole fibres per thread leave (ts*q - F) of ts*q lanes idle, and the FP64 pipe
+            // is charged per warp instruction whatever the number of active lanes.  FP64
+            // maps output elements to threads instead (fwd_single_elem_kernel) when that
+            // uses the lanes clearly better: teams are the smallest power of two that gives
+            // every thread at most 4 elements (2-4 elements per thread measured 5-25 %
+            // faster than 6-16 on d = 3..6, n = 3..7: shorter chains per mode), and the
+            // element mapping is taken when its lane use beats the fibre mapping's by more
+            // than 5 points.  Measured on 128 MB batches: d = 3, n = 6 -22 %; d = 3, n = 5
+            // -24 %; d = 2, n = 4 -27 %; d = 3, n = 3 / 7 and d = 5, n = 3 -14..-17 %
+            // (n = 3, 5, 7 against an element kernel with n known only at run time); where
+            // the lane use is equal (d = 2, n = 6..8; d = 4, n = 4..6) the fibre kernels were
+            // as fast or up to 16 % faster.
             const double fibre_util = (double)F / ((double)ts * ((F + ts - 1) / ts));
-            if (sizeof(T) == 8 && (n & 1) && fibre_util < 0.9 && !(tune && tune->team_size > 0)) {
-                const int best_ts = elem_team_size(N, 16, 0, 256);
-                const double best =
-                    best_ts ? (double)N / ((double)best_ts * ((N + best_ts - 1) / best_ts)) : 0.0;
-                if (best_ts > 0 && best > fibre_util) {
-                    const int per = (N + best_ts - 1) / best_ts;
+            if (sizeof(T) == 8 && !(tune && tune->team_size > 0)) {
+                int tse = 8;
+                while (tse < 256 && (N + tse - 1) / tse > 4) tse *= 2;
+                const int per = (N + tse - 1) / tse;
+                const double util_e = (double)N / ((double)tse * per);
+                if (per <= 8 && util_e > fibre_util + 0.05) {  // at most 8 elements: no spills
                     int emax = 1;
                     while (emax < per) emax *= 2;
-                    auto fe = fwd_single_elem_lookup<T, TO>(emax);
+                    auto fe = fwd_single_elem_lookup<T, TO>(n, emax);
                     if (fe) {
                         fn = fe;
-                        ts = best_ts;
+                        ts = tse;
                         teams = 256 / ts;
                     }
                 }

@@ -145,3 +145,26 @@ def build_drop_in(tmp_dir):
 
 def test_cpp_drop_in_compiles(lib, tmp_path):
     assert os.path.exists(build_drop_in(tmp_path))
+
+
+def test_host_pipeline_piece_plan():
+    """Host pipelines cut their pieces at output-group starts: even pieces, or a last
+    piece holding `last_share` of the groups; every piece non-empty, cuts increasing."""
+    from kronmult_gb300 import DeviceBatch
+    from kronmult_gb300 import workloads as W
+    from kronmult_gb300.api import _host_pipeline_plan
+
+    b = W.config2(scale=24 / 4096)  # 24 output groups of 9 entries
+    db = DeviceBatch.from_host(b, device="cpu")
+    assert _host_pipeline_plan(db, 2)[0] == [0, 108, 216]
+    assert _host_pipeline_plan(db, 2, 0.1)[0] == [0, 198, 216]
+    assert _host_pipeline_plan(db, 3, 0.1)[0] == [0, 99, 198, 216]
+    for chunks in (1, 2, 3, 7, 24, 40):
+        for share in (None, 0.01, 0.1, 0.5, 0.99):
+            cuts, _, out_rows, _, _ = _host_pipeline_plan(db, chunks, share)
+            assert cuts[0] == 0 and cuts[-1] == b.nb
+            assert all(lo < hi and lo % 9 == 0 for lo, hi in zip(cuts, cuts[1:]))
+            assert len(cuts) - 1 == min(chunks, 24)
+            assert out_rows[0][0] == 0 and out_rows[-1][1] == 24
+    with pytest.raises(ValueError):
+        _host_pipeline_plan(db, 2, 1.0)

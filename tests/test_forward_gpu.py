@@ -333,3 +333,22 @@ def test_edge_shapes(cuda, d, n, dtype):
     got, _ = run(b, cuda, dtype=dtype)
     tol = TOL64 if dtype == torch.float64 else TOL32
     assert O.rel_l2(got, O.forward(b)) <= tol
+
+
+@pytest.mark.parametrize("d,n", [(3, 6), (3, 3), (2, 4), (3, 5), (5, 3), (3, 7), (4, 4), (2, 6), (4, 5)])
+def test_fp64_element_and_fibre_mappings_agree_bitwise(cuda, d, n):
+    """FP64 maps output elements to threads where whole fibres would idle lanes
+    (d = 3, n = 6; d = 2, n = 4; ...) and whole fibres elsewhere; both run the same
+    k-ascending FMA chain per element, so with one entry per output the default
+    launch and a launch forced onto fibres (a fixed team size) agree bit for bit."""
+    from kronmult_gb300 import DeviceBatch
+    from kronmult_gb300 import workloads as W
+
+    b = W.make_batch(d, n, n, 300, 1, seed=4000 + 10 * d + n)
+    outs = []
+    for tuning in (None, {"team_size": 16}):
+        db = DeviceBatch.from_host(b, device=cuda, dtype=torch.float64)
+        db.forward(tuning=tuning, sync=True)
+        outs.append(db.outputs.cpu().numpy())
+    assert np.array_equal(outs[0], outs[1])
+    assert O.rel_l2(outs[0], O.forward(b)) <= TOL64
