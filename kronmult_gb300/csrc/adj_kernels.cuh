@@ -39,11 +39,26 @@ template <typename T> struct AdjArgs {
     int d, n, stride, gstride;
     int N;
     int team_size, teams_per_cta, entries_per_team;
+    long long balanced_teams;  // > 0: team t takes entries [t*nb/B, (t+1)*nb/B) of B teams
     int team_elems;         // elements of T per team slice
     int npad;               // padded vector length
     int store_all;          // 1: keep all d partial products; 0: rebuild each from x
     int slices;             // split of the grad contraction over the team
 };
+
+// Entries of one team: contiguous ranges of (nearly) equal length over every team
+// slot of the grid, or fixed runs of entries_per_team.
+template <typename T>
+__device__ __forceinline__ void adj_team_range(const AdjArgs<T> &a, long long team, long long &b, long long &e)
+{
+    if (a.balanced_teams > 0) {
+        b = team * a.nb / a.balanced_teams;
+        e = (team + 1) * a.nb / a.balanced_teams;
+    } else {
+        b = team * a.entries_per_team;
+        e = min(b + (long long)a.entries_per_team, a.nb);
+    }
+}
 
 // Every phase maps threads to individual output elements (not to whole fibres), so
 // that all lanes of a warp have work for any n: with n = 6 and 32-thread teams a
@@ -126,8 +141,8 @@ __global__ void __launch_bounds__(512) adj_elem_kernel(const AdjArgs<T> a)
     const bool want_gA = a.gmats != nullptr;
 
     const long long team_global = (long long)blockIdx.x * a.teams_per_cta + tm.id;
-    long long e = team_global * a.entries_per_team;
-    const long long e_end = min(e + (long long)a.entries_per_team, a.nb);
+    long long e, e_end;
+    adj_team_range(a, team_global, e, e_end);
     if (e >= e_end) return;
 
     if (want_gA) {
@@ -308,8 +323,8 @@ __global__ void __launch_bounds__(256, 3) adj_smem_kernel(const AdjArgs<T> a)
     const bool want_gA = a.gmats != nullptr;
 
     const long long team_global = (long long)blockIdx.x * a.teams_per_cta + tm.id;
-    long long e = team_global * a.entries_per_team;
-    const long long e_end = min(e + (long long)a.entries_per_team, a.nb);
+    long long e, e_end;
+    adj_team_range(a, team_global, e, e_end);
     if (e >= e_end) return;
 
     if (want_gA) {

@@ -185,9 +185,18 @@ static int adjoint_async(int d, int n, const T *const *mats, int stride, const T
                                                          : (nb + total_teams - 1) / total_teams;
     if (ept < 1) ept = 1;
     if (ept > INT_MAX) ept = INT_MAX;
-    const long long grid = (nb + ept * teams - 1) / (ept * teams);
+    long long grid = (nb + ept * teams - 1) / (ept * teams);
+    // more entries than team slots and no tuned run length: every slot of one full
+    // wave takes an equal share (runs of ept entries left up to a quarter of the slots
+    // idle: d = 3, n = 6, FP32, 16384 entries on 7296 slots)
+    long long balanced = 0;
+    if (!(tune && tune->entries_per_team > 0) && nb > total_teams) {
+        balanced = total_teams;
+        grid = (long long)di.sms * per_sm;
+    }
     if (grid > INT_MAX) return cudaErrorInvalidValue;
     AdjArgs<T> a{};
+    a.balanced_teams = balanced;
     a.mats = mats;
     a.in = in;
     a.gout = gout;
