@@ -5,17 +5,20 @@
 //     Y[c + r*F] = sum_k A_i(r, k) X[k + 8c],   F = N/8 fibres
 // is a dense GEMM D[c][r] = sum_k X^T[c][k] A_i^T[k][r] with M = F, N = 8, K = 8.
 // It runs as tcgen05.mma.cta_group::1 with M = 128 fibres per instruction
-// (N padded to 16, the smallest N for M = 128; K = 8 for TF32, K = 16 for BF16
-// with the upper 8 zero).  Operands live in shared memory in the canonical
-// K-major, no-swizzle layout of 8-row x 16-byte core matrices; the accumulator
-// lives in tensor memory, one 16-column block per 128-fibre tile.  After each
-// mode the four warps read their 32 TMEM lanes (tcgen05.ld.32x32b), round to the
-// operand type and write the mode output straight into the next mode's operand
-// layout at the rotated positions, so the vector never leaves shared memory.
+// (N = 16, the smallest N for M = 128; K = 8 for TF32, K = 16 for BF16 with the
+// upper 8 zero).  Operands live in shared memory in the canonical K-major,
+// no-swizzle layout of 8-row x 16-byte core matrices; the accumulator lives in
+// tensor memory, one 16-column block per PAIR of 128-fibre tiles: the even tile
+// multiplies B = [A_i^T | 0] into columns 0..7, the odd tile B = [0 | A_i^T]
+// accumulated into columns 8..15, so no accumulator column is padding and a CTA
+// needs half the columns (more CTAs per SM).  After each mode the four warps read
+// their 32 TMEM lanes (tcgen05.ld.32x32b), round to the operand type and write
+// the mode output straight into the next mode's operand layout at the rotated
+// positions, so the vector never leaves shared memory.
 //
 // One CTA = one warpgroup (128 threads) works on one entry at a time; several
 // CTAs per SM overlap the input loads.  Consecutive entries with the same
-// output pointer are summed in FP32 registers and added with FP64 atomics.
+// output pointer are summed in tensor memory and added with FP64 atomics.
 //
 // Every wait on an mbarrier is bounded; on timeout the kernel records an error
 // code in a device word (kronmult_device_error) and leaves after freeing its
@@ -117,14 +120,20 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase, unsigne
     return false;
 }
 
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8])
+// 16 consecutive columns of this warp's 32 lanes: the two tiles of one block
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v0)[8], float (&v1)[8])
 {
-    uint32_t r[8];
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-                 : "r"(taddr));
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
 #pragma unroll
-    for (int j = 0; j < 8; ++j) v[j] = __uint_as_float(r[j]);
+    for (int j = 0; j < 8; ++j) {
+        v0[j] = __uint_as_float(r[j]);
+        v1[j] = __uint_as_float(r[8 + j]);
+    }
 }
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
@@ -180,14 +189,16 @@ __device__ __forceinline__ void tc_load_ptrs(TcPtrs &p, const TcArgs &a, long lo
     }
 }
 
-// asynchronous copy of one entry into a raw staging slot: the vector in natural
-// order, the factors as fraw[i*64 + r + 8k] = A_i(r, k).  The vector is one TMA bulk
-// copy (cp.async.bulk) issued by thread 0 and completed on the staging barrier `sbar`
-// when its source is 16-byte aligned; otherwise every thread copies 4-byte elements
-// with cp.async and thread 0 completes the barrier's phase without bytes.  Either way
-// the staging barrier completes exactly one phase per entry.
-__device__ __forceinline__ void tc_stage_async(float *raw, float *fraw, const TcPtrs &p, const TcArgs &a, int tid,
-                                               uint32_t sbar)
+// asynchronous copy of one entry's vector into the raw staging slot (natural order)
+// and of its factor elements into registers: thread tid holds fv[s] = A_i(r, k) for
+// idx = tid + 128 s, i = idx / 64, r = idx % 8, k = (idx / 8) % 8.  The vector is one TMA
+// bulk copy (cp.async.bulk) issued by thread 0 and completed on the staging barrier
+// `sbar` when its source is 16-byte aligned; otherwise every thread copies 4-byte
+// elements with cp.async and thread 0 completes the barrier's phase without bytes.
+// Either way the staging barrier completes exactly one phase per entry.  The factor
+// loads are plain loads consumed one entry later, so their latency is hidden too.
+__device__ __forceinline__ void tc_stage_async(float *raw, float (&fv)[kTcFacSlots], const TcPtrs &p,
+                                               const TcArgs &a, int tid, uint32_t sbar)
 {
     const int N = a.N;
     const unsigned bytes = (unsigned)N * 4u;
@@ -205,29 +216,28 @@ __device__ __forceinline__ void tc_stage_async(float *raw, float *fraw, const Tc
         for (int q = tid; q < N; q += kTcThreads) cp_async<4>(raw + q, p.src + q);
         if (tid == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(sbar) : "memory");
     }
+    cp_async_commit();
 #pragma unroll
     for (int s = 0; s < kTcFacSlots; ++s) {
         const int idx = tid + s * kTcThreads;
         if (idx < a.d * 64) {
             const int r = idx & 7, k = (idx >> 3) & 7;
-            cp_async<4>(fraw + idx, p.mat[s] + r + (size_t)k * a.stride);
+            fv[s] = __ldg(p.mat[s] + r + (size_t)k * a.stride);
         }
     }
-    cp_async_commit();
 }
 
-template <int KIND> __global__ void __launch_bounds__(kTcThreads, 4) fwd_tc_kernel(const TcArgs a)
+template <int KIND> __global__ void __launch_bounds__(kTcThreads, 6) fwd_tc_kernel(const TcArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int N = a.N, F = N / 8, d = a.d;
-    // shared memory: two raw staging slots (vector + factors), operand A, operand B, barrier
-    float *raw0 = reinterpret_cast<float *>(smem_raw);
-    float *fraw0 = raw0 + N;
-    float *raw1 = fraw0 + d * 64;
-    float *fraw1 = raw1 + N;
-    unsigned char *xs = reinterpret_cast<unsigned char *>(fraw1 + d * 64);  // tiles x 4 KB
-    unsigned char *bs = xs + (size_t)a.tiles * kTileBytes + 64;             // d x 512 B
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(bs + (size_t)d * kBBytes);  // MMA completion
+    // shared memory: one raw staging slot for the vector, operand A, operands B, barriers.
+    // The slot is refilled with the next entry as soon as this entry's operands are built.
+    float *raw = reinterpret_cast<float *>(smem_raw);
+    unsigned char *xs = reinterpret_cast<unsigned char *>(raw + N);  // tiles x 4 KB
+    unsigned char *bs = xs + (size_t)a.tiles * kTileBytes + 64;            // d x 512 B: [A_i^T | 0]
+    unsigned char *bs2 = bs + (size_t)d * kBBytes;                         // d x 512 B: [0 | A_i^T]
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(bs2 + (size_t)d * kBBytes);  // MMA completion
     uint64_t *sbar = mbar + 1;                                                  // staging completion
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 2);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -236,8 +246,9 @@ template <int KIND> __global__ void __launch_bounds__(kTcThreads, 4) fwd_tc_kern
     const long long e_end = min(e + (long long)a.entries_per_cta, a.nb);
     if (e >= e_end) return;
 
-    // operands zeroed once: padding rows of B (8..15) and, for BF16, the K 8..15 half of A stay zero
-    for (int v = tid; v < (a.tiles * kTileBytes + 64 + d * kBBytes) / 16; v += kTcThreads)
+    // operands zeroed once: the zero half of each B (rows 8..15 of [A^T | 0], rows 0..7 of
+    // [0 | A^T]) and, for BF16, the K 8..15 half of A stay zero
+    for (int v = tid; v < (a.tiles * kTileBytes + 64 + 2 * d * kBBytes) / 16; v += kTcThreads)
         reinterpret_cast<int4 *>(xs)[v] = make_int4(0, 0, 0, 0);
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
@@ -252,16 +263,18 @@ template <int KIND> __global__ void __launch_bounds__(kTcThreads, 4) fwd_tc_kern
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     TcPtrs nxt;
+    float fv[kTcFacSlots] = {0.f, 0.f};  // factor elements of the entry staged last
     tc_load_ptrs(nxt, a, e, tid);
-    tc_stage_async(raw0, fraw0, nxt, a, tid, sbar_a);
+    tc_stage_async(raw, fv, nxt, a, tid, sbar_a);
     if (e + 1 < e_end) tc_load_ptrs(nxt, a, e + 1, tid);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    const uint32_t tacc = tmem + 16u * a.tiles;  // run accumulator: one 16-column block per tile
+    const int blocks = (a.tiles + 1) / 2;        // 16-column accumulator blocks, two tiles each
+    const uint32_t tacc = tmem + 16u * blocks;   // run accumulator after the mode output
     const uint32_t mbar_a = smem_u32(mbar);
-    const uint32_t xs_a = smem_u32(xs), bs_a = smem_u32(bs);
+    const uint32_t xs_a = smem_u32(xs), bs_a = smem_u32(bs), bs2_a = smem_u32(bs2);
     const uint32_t lboa = a_lbo(a.tiles);  // A operand: k-chunk-1 core matrices this far after chunk 0
     uint32_t phase = 0, sphase = 0;
     bool failed = false;
@@ -271,22 +284,25 @@ template <int KIND> __global__ void __launch_bounds__(kTcThreads, 4) fwd_tc_kern
 
     // run sum (TMEM accumulator) -> FP64 atomics into `dst`
     auto flush = [&](double *dst) {
-        float v[MAXT][8];
-#pragma unroll
-        for (int t = 0; t < MAXT; ++t)
-            if (t < a.tiles) tmem_ld8(tacc + ((uint32_t)(warp * 32) << 16) + 16u * t, v[t]);
-        tmem_wait_ld();
-#pragma unroll
-        for (int t = 0; t < MAXT; ++t) {
+        auto add_tile = [&](int t, const float (&v)[8]) {
             const int c = t * kTileRows + warp * 32 + lane;
             if (t < a.tiles && c < F)
 #pragma unroll
-                for (int r = 0; r < 8; ++r) atomicAdd(dst + c + r * F, (double)v[t][r]);
+                for (int r = 0; r < 8; ++r) atomicAdd(dst + c + r * F, (double)v[r]);
+        };
+#pragma unroll
+        for (int j = 0; j < MAXT / 2; ++j) {
+            if (j < blocks) {
+                float v0[8], v1[8];
+                tmem_ld16(tacc + ((uint32_t)(warp * 32) << 16) + 16u * j, v0, v1);
+                tmem_wait_ld();
+                add_tile(2 * j, v0);
+                add_tile(2 * j + 1, v1);
+            }
         }
     };
 
-    for (int slot = 0; e < e_end; ++e, slot ^= 1) {
-        float *raw = slot ? raw1 : raw0, *fraw = slot ? fraw1 : fraw0;
+    for (; e < e_end; ++e) {
         double *o = a.out[e];
         cp_async_wait_all();
         const bool staged = mbar_wait(sbar_a, sphase);  // the slot's bulk copy (or its empty phase)
@@ -297,15 +313,16 @@ template <int KIND> __global__ void __launch_bounds__(kTcThreads, 4) fwd_tc_kern
         }
         sphase ^= 1u;
         staging = false;
-        if (e + 1 < e_end) {
-            tc_stage_async(slot ? raw0 : raw1, slot ? fraw0 : fraw1, nxt, a, tid, sbar_a);
-            staging = true;
-            if (e + 2 < e_end) tc_load_ptrs(nxt, a, e + 2, tid);
-        }
-        // operands: B_i[row r][k] = A_i(r, k); input natural index p = k + 8c -> A row c, column k
-        for (int v = tid; v < d * 64; v += kTcThreads) {
-            const int i = v >> 6, r = v & 7, k = (v >> 3) & 7;
-            put<KIND>(bs + (size_t)i * kBBytes, r, k, fraw[v]);
+        // operands: B_i[row r][k] = A_i(r, k) (and row r + 8 of the second copy); input
+        // natural index p = k + 8c -> A row c, column k
+#pragma unroll
+        for (int s = 0; s < kTcFacSlots; ++s) {
+            const int v = tid + s * kTcThreads;
+            if (v < d * 64) {
+                const int i = v >> 6, r = v & 7, k = (v >> 3) & 7;
+                put<KIND>(bs + (size_t)i * kBBytes, r, k, fv[s]);
+                put<KIND>(bs2 + (size_t)i * kBBytes, r + 8, k, fv[s]);
+            }
         }
         for (int q = tid; q < N / 4; q += kTcThreads) {
             const float4 v4 = *reinterpret_cast<const float4 *>(raw + 4 * q);
@@ -320,18 +337,25 @@ template <int KIND> __global__ void __launch_bounds__(kTcThreads, 4) fwd_tc_kern
         const bool cont = (o == cur);
         if (!cont && cur != nullptr) flush(cur);
         cur = o;
-        fence_async_smem();
+        fence_async_smem();  // the staging slot has been read (generic proxy) before the bulk copy refills it
         tc_fence_before();
         __syncthreads();
+        if (e + 1 < e_end) {
+            tc_stage_async(raw, fv, nxt, a, tid, sbar_a);
+            staging = true;
+            if (e + 2 < e_end) tc_load_ptrs(nxt, a, e + 2, tid);
+        }
 
         for (int i = d - 1; i >= 0; --i) {
             if (tid == 0) {
                 tc_fence_after();
                 const uint32_t dst = i > 0 ? tmem : tacc;
                 const uint32_t accumulate = (i == 0 && cont) ? 1u : 0u;
+                // even tile: columns 0..7 of its block (overwriting, or adding to the run);
+                // odd tile: columns 8..15, always added (the even tile's B zeroed them)
                 for (int t = 0; t < a.tiles; ++t)
-                    mma<KIND>(dst + 16u * t, smem_desc(xs_a + t * 2048u, lboa, 128u), smem_desc(bs_a + i * kBBytes),
-                              accumulate);
+                    mma<KIND>(dst + 16u * (uint32_t)(t >> 1), smem_desc(xs_a + t * 2048u, lboa, 128u),
+                              smem_desc(((t & 1) ? bs2_a : bs_a) + i * kBBytes), (t & 1) ? 1u : accumulate);
                 mma_commit(mbar_a);
             }
             const bool ok = mbar_wait(mbar_a, phase);
@@ -344,22 +368,27 @@ template <int KIND> __global__ void __launch_bounds__(kTcThreads, 4) fwd_tc_kern
             phase ^= 1u;
             tc_fence_after();
             if (i > 0) {
-                float v[MAXT][8];
-#pragma unroll
-                for (int t = 0; t < MAXT; ++t)
-                    if (t < a.tiles) tmem_ld8(tmem + ((uint32_t)(warp * 32) << 16) + 16u * t, v[t]);
-                tmem_wait_ld();
                 // mode output element (row c, r) goes to natural position p = c + r*F,
-                // which is operand row p/8, column p%8 of the next mode
-#pragma unroll
-                for (int t = 0; t < MAXT; ++t) {
+                // which is operand row p/8, column p%8 of the next mode; one block (two
+                // tiles) at a time keeps 16 values per thread live
+                auto store_tile = [&](int t, const float (&v)[8]) {
                     const int c = t * kTileRows + warp * 32 + lane;
                     if (t < a.tiles && c < F) {
 #pragma unroll
                         for (int r = 0; r < 8; ++r) {
                             const uint32_t p = c + r * F;
-                            put<KIND>(xs, p >> 3, p & 7, v[t][r], lboa);
+                            put<KIND>(xs, p >> 3, p & 7, v[r], lboa);
                         }
+                    }
+                };
+#pragma unroll
+                for (int j = 0; j < MAXT / 2; ++j) {
+                    if (j < blocks) {
+                        float v0[8], v1[8];
+                        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + 16u * j, v0, v1);
+                        tmem_wait_ld();
+                        store_tile(2 * j, v0);
+                        store_tile(2 * j + 1, v1);
                     }
                 }
                 fence_async_smem();
@@ -403,10 +432,10 @@ int launch_tc_forward(int kind, int d, int n, const float *const *mats, int stri
     const int F = a.N / 8;
     a.tiles = (F + kTileRows - 1) / kTileRows;
     int cols = 32;
-    while (cols < 2 * 16 * a.tiles) cols *= 2;  // mode output + run accumulator
+    while (cols < 2 * 16 * ((a.tiles + 1) / 2)) cols *= 2;  // mode output + run accumulator
     a.tmem_cols = cols;
-    const size_t need = (size_t)2 * (a.N + d * 64) * sizeof(float) + (size_t)a.tiles * kTileBytes + 64 +
-                        (size_t)d * kBBytes + 32;  // + two mbarriers and the TMEM address
+    const size_t need = (size_t)a.N * sizeof(float) + (size_t)a.tiles * kTileBytes + 64 +
+                        (size_t)2 * d * kBBytes + 32;  // + two mbarriers and the TMEM address
     // resident CTAs per SM are limited so that their tensor-memory columns fit in 512:
     // each CTA reserves 1/max_ctas of the SM's shared memory (less the per-CTA system
     // reservation), so exactly max_ctas fit
