@@ -436,10 +436,11 @@ int launch_tc_forward(int kind, int d, int n, const float *const *mats, int stri
     a.tmem_cols = cols;
     const size_t need = (size_t)a.N * sizeof(float) + (size_t)a.tiles * kTileBytes + 64 +
                         (size_t)2 * d * kBBytes + 32;  // + two mbarriers and the TMEM address
-    // resident CTAs per SM are limited so that their tensor-memory columns fit in 512:
-    // each CTA reserves 1/max_ctas of the SM's shared memory (less the per-CTA system
-    // reservation), so exactly max_ctas fit
-    const int max_ctas = 512 / cols;
+    // resident CTAs per SM are limited so that their tensor-memory columns fit in 512
+    // (or to tuning.ctas_per_sm when that is fewer): each CTA reserves 1/max_ctas of the
+    // SM's shared memory (less the per-CTA system reservation), so at most max_ctas fit
+    int max_ctas = 512 / cols;
+    if (tune && tune->ctas_per_sm > 0 && tune->ctas_per_sm < max_ctas) max_ctas = tune->ctas_per_sm;
     size_t smem = (size_t)di.smem_per_sm / max_ctas - (size_t)di.smem_reserved_cta;
     smem &= ~(size_t)15;
     if (smem < need) smem = need;
