@@ -136,3 +136,25 @@ def test_tc_unaligned_inputs(cuda, compute):
     torch.cuda.synchronize()
     assert ctypes_device_error() == 0
     assert O.rel_l2(db.outputs.cpu().numpy(), O.forward(b)) <= TOL[compute]
+
+
+@pytest.mark.parametrize("compute", ["tf32", "bf16"])
+@pytest.mark.parametrize("tuning", [{"ctas_per_sm": 3}, {"ctas_per_sm": 5, "entries_per_team": 3},
+                                    {"entries_per_team": 1}])
+def test_tc_launch_shapes(cuda, compute, tuning):
+    """Fewer resident CTAs per SM (the shared-memory reservation grows) and other run
+    lengths per CTA: the same values as the default launch up to FP64 summation order."""
+    from kronmult_gb300 import DeviceBatch, _lib, forward_f32_f64out
+    from kronmult_gb300 import workloads as W
+
+    code = {"tf32": _lib.KRONMULT_COMPUTE_TF32, "bf16": _lib.KRONMULT_COMPUTE_BF16}[compute]
+    b = W.config4(scale=24 / 4096)
+    outs = []
+    for t in (None, tuning):
+        db = DeviceBatch.from_host(b, device=cuda, dtype=torch.float32, out_dtype=torch.float64)
+        forward_f32_f64out(db, compute=code, tuning=t)
+        torch.cuda.synchronize()
+        assert ctypes_device_error() == 0
+        outs.append(db.outputs.cpu().numpy())
+    assert O.rel_l2(outs[1], outs[0]) <= 1e-12
+    assert O.rel_l2(outs[0], O.forward(b)) <= TOL[compute]
