@@ -142,8 +142,10 @@ def test_tc_unaligned_inputs(cuda, compute):
 @pytest.mark.parametrize("tuning", [{"ctas_per_sm": 3}, {"ctas_per_sm": 5, "entries_per_team": 3},
                                     {"entries_per_team": 1}])
 def test_tc_launch_shapes(cuda, compute, tuning):
-    """Fewer resident CTAs per SM (the shared-memory reservation grows) and other run
-    lengths per CTA: the same values as the default launch up to FP64 summation order."""
+    """Fewer resident CTAs per SM (the shared-memory reservation grows): the same values
+    as the default launch up to FP64 summation order.  Other run lengths per CTA change
+    which consecutive entries are summed in FP32 in tensor memory before the FP64
+    atomics: equal up to FP32 rounding of those sums."""
     from kronmult_gb300 import DeviceBatch, _lib, forward_f32_f64out
     from kronmult_gb300 import workloads as W
 
@@ -156,5 +158,5 @@ def test_tc_launch_shapes(cuda, compute, tuning):
         torch.cuda.synchronize()
         assert ctypes_device_error() == 0
         outs.append(db.outputs.cpu().numpy())
-    assert O.rel_l2(outs[1], outs[0]) <= 1e-12
+    assert O.rel_l2(outs[1], outs[0]) <= (1e-6 if "entries_per_team" in tuning else 1e-12)
     assert O.rel_l2(outs[0], O.forward(b)) <= TOL[compute]
