@@ -88,18 +88,99 @@ __device__ __forceinline__ double f2d_scaled(float f, int s)
                                             ((unsigned long long)(b & 0x7FFFFF) << 29)));
 }
 
+// Packed FP32 pairs (sm_100 family: add / sub / mul / fma .rn.f32x2): two independent
+// lanes per instruction, each rounded exactly as the scalar operation (the FP32 pipe's
+// rate is unchanged; the instructions to issue are halved).
+using f2 = unsigned long long;
+__device__ __forceinline__ f2 f2_pack(float lo, float hi)
+{
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(f2 v, float &lo, float &hi)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f2 f2_add(f2 a, f2 b)
+{
+    f2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 f2_sub(f2 a, f2 b)
+{
+    f2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 f2_mul(f2 a, f2 b)
+{
+    f2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 f2_fma(f2 a, f2 b, f2 c)
+{
+    f2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ f2 f2_neg(f2 a) { return a ^ 0x8000000080000000ull; }
+
+// rows r, r + 1 of a column-major factor column: one 8-byte load when NN is even (r
+// even, the factor arrays 8-byte aligned), two 4-byte loads otherwise
+template <int NN> __device__ __forceinline__ f2 f2_rows(const float *p)
+{
+    if constexpr (NN % 2 == 0) {
+        return *reinterpret_cast<const f2 *>(p);
+    } else {
+        return f2_pack(p[0], p[1]);
+    }
+}
+
 // y = M . b for one fibre in double-float arithmetic: M (hi/lo) col-major NN x NN,
 // b and y as hi/lo pairs.  Every output is the k-ascending sum of exact products,
-// accumulated with two-sums and renormalised once.
+// accumulated with two-sums and renormalised once.  Rows are computed two at a time
+// in packed pairs (the same operations per row as the scalar form for an odd last row).
 template <int NN>
 __device__ __forceinline__ void df_fibre(const float *Mh, const float *Ml, const float (&bh)[NN],
                                          const float (&bl)[NN], float (&yh)[NN], float (&yl)[NN])
 {
 #pragma unroll
-    for (int r = 0; r < NN; ++r) {
+    for (int r = 0; r + 1 < NN; r += 2) {
+        // k = 0: the sum starts as the exact product
+        f2 ah = f2_rows<NN>(Mh + r), al = f2_rows<NN>(Ml + r);
+        f2 b_h = f2_pack(bh[0], bh[0]), b_l = f2_pack(bl[0], bl[0]);
+        f2 sh = f2_mul(ah, b_h);
+        f2 sl = f2_fma(ah, b_h, f2_neg(sh));
+        sl = f2_fma(ah, b_l, sl);
+        sl = f2_fma(al, b_h, sl);
+#pragma unroll
+        for (int k = 1; k < NN; ++k) {
+            ah = f2_rows<NN>(Mh + r + k * NN);
+            al = f2_rows<NN>(Ml + r + k * NN);
+            b_h = f2_pack(bh[k], bh[k]);
+            b_l = f2_pack(bl[k], bl[k]);
+            const f2 p = f2_mul(ah, b_h);  // two-product: p + ep = ah*bh exactly
+            f2 ep = f2_fma(ah, b_h, f2_neg(p));
+            ep = f2_fma(ah, b_l, ep);      // cross terms
+            ep = f2_fma(al, b_h, ep);
+            const f2 t = f2_add(sh, p);    // two-sum: t + err = sh + p exactly
+            const f2 bp = f2_sub(t, sh);
+            const f2 err = f2_add(f2_sub(sh, f2_sub(t, bp)), f2_sub(p, bp));
+            sh = t;
+            sl = f2_add(sl, f2_add(err, ep));
+        }
+        const f2 h = f2_add(sh, sl);  // renormalise: h + l = sh + sl
+        const f2 l = f2_sub(sl, f2_sub(h, sh));
+        f2_unpack(h, yh[r], yh[r + 1]);
+        f2_unpack(l, yl[r], yl[r + 1]);
+    }
+    if constexpr (NN % 2 == 1) {
+        constexpr int r = NN - 1;
         // The error-free steps use explicitly rounded operations so that the
         // compiler cannot fuse a product into a later addition.
-        // k = 0: the sum starts as the exact product
         float ah = Mh[r], al = Ml[r];
         float sh = __fmul_rn(ah, bh[0]);
         float sl = fmaf(ah, bh[0], -sh);
@@ -109,17 +190,17 @@ __device__ __forceinline__ void df_fibre(const float *Mh, const float *Ml, const
         for (int k = 1; k < NN; ++k) {
             ah = Mh[r + k * NN];
             al = Ml[r + k * NN];
-            const float p = __fmul_rn(ah, bh[k]);  // two-product: p + ep = ah*bh exactly
+            const float p = __fmul_rn(ah, bh[k]);
             float ep = fmaf(ah, bh[k], -p);
-            ep = fmaf(ah, bl[k], ep);              // cross terms
+            ep = fmaf(ah, bl[k], ep);
             ep = fmaf(al, bh[k], ep);
-            const float t = __fadd_rn(sh, p);      // two-sum: t + err = sh + p exactly
+            const float t = __fadd_rn(sh, p);
             const float bp = __fsub_rn(t, sh);
             const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(p, bp));
             sh = t;
             sl = __fadd_rn(sl, __fadd_rn(err, ep));
         }
-        const float h = __fadd_rn(sh, sl);  // renormalise: h + l = sh + sl
+        const float h = __fadd_rn(sh, sl);
         yl[r] = __fsub_rn(sl, __fsub_rn(h, sh));
         yh[r] = h;
     }
