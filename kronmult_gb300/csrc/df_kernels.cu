@@ -88,46 +88,6 @@ __device__ __forceinline__ double f2d_scaled(float f, int s)
                                             ((unsigned long long)(b & 0x7FFFFF) << 29)));
 }
 
-// Packed FP32 pairs (sm_100 family: add / sub / mul / fma .rn.f32x2): two independent
-// lanes per instruction, each rounded exactly as the scalar operation (the FP32 pipe's
-// rate is unchanged; the instructions to issue are halved).
-using f2 = unsigned long long;
-__device__ __forceinline__ f2 f2_pack(float lo, float hi)
-{
-    f2 r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-    return r;
-}
-__device__ __forceinline__ void f2_unpack(f2 v, float &lo, float &hi)
-{
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
-__device__ __forceinline__ f2 f2_add(f2 a, f2 b)
-{
-    f2 d;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ f2 f2_sub(f2 a, f2 b)
-{
-    f2 d;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ f2 f2_mul(f2 a, f2 b)
-{
-    f2 d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ f2 f2_fma(f2 a, f2 b, f2 c)
-{
-    f2 d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-    return d;
-}
-__device__ __forceinline__ f2 f2_neg(f2 a) { return a ^ 0x8000000080000000ull; }
-
 // rows r, r + 1 of a column-major factor column: one 8-byte load when NN is even (r
 // even, the factor arrays 8-byte aligned), two 4-byte loads otherwise
 template <int NN> __device__ __forceinline__ f2 f2_rows(const float *p)
