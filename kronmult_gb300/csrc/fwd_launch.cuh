@@ -258,7 +258,7 @@ int plan_forward(FwdPlan<T, TO> &pl, int d, int n, const T *const *mats, int str
             // element mapping is taken when its lane use beats the fibre mapping's by more
             // than 5 points.  Measured on 128 MB batches: d = 3, n = 6 -22 %; d = 3, n = 5
             // -24 %; d = 2, n = 4 -27 %; d = 3, n = 3 / 7 and d = 5, n = 3 -14..-17 %
-            // (n = 3, 5, 7 against an element kernel with n known only at run time); where
+            // (for odd n the baseline was an element kernel taking n at run time); where
             // the lane use is equal (d = 2, n = 6..8; d = 4, n = 4..6) the fibre kernels were
             // as fast or up to 16 % faster.
             const double fibre_util = (double)F / ((double)ts * ((F + ts - 1) / ts));
