@@ -6,7 +6,7 @@ Default workload: the plain FP64 forward at d=6, n=4 (N=4096), matrix_stride 8,
 whole batch.  Prints one JSON line.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--config c1|c2|c4|c5] [--dtype f64|f32]
+                  [--config c1|c2|c4|c5] [--dtype f64|f32] [--scaling strong|weak]
 
 value       GFLOP/s (algorithmic 2*d*n*N flops per entry) over K device-timed steps,
             inputs resident in HBM (the 1.2 GB input set is 9x the 129 MB L2, so no
@@ -19,10 +19,16 @@ e2e         the same metric through the public API with host (pinned) buffers:
             from pinned host memory (api.forward_from_host_mapped)
 roofline    the forward kernel against the roof that binds it; for FP64 that is the
             FP64 FMA pipe, measured live (HBM fraction reported beside it)
-cpu_baseline  the C oracle (a restatement of the reference's kronmult_omp) on the
-            host cores, same workload
---impl reference  the reference's CPU algorithm (oracle port; the reference sources are
-            not present on the GPU host) timed on all host cores
+cpu_baseline  the reference's own kronmult_omp (built from its sources into oracle/_ref,
+            rebuilt for the host's architecture from the staged sources) on all host
+            cores, same workload; the C restatement of it only where that build cannot
+            be made, which the line then says
+--impl reference  the same reference build timed on all host cores, on this arm's
+            workload, metric and config (rank 0 alone under torchrun)
+N > 1       one process per GPU; by default one seeded batch is cut into shards at
+            output-group boundaries (sharding.shard_batch), so no collective is needed
+            and `value` is the whole batch's flops over the slowest rank's time
+            ("strong"); --scaling weak gives every rank a full-size batch of its own
 """
 from __future__ import annotations
 
@@ -63,6 +69,9 @@ def parse():
                    help="measure every configuration, one JSON line each (diagnostic report)")
     p.add_argument("--only", default="",
                    help="with --suite: run only the items whose name starts with this prefix (c1, c2, c3, c4, c5)")
+    p.add_argument("--scaling", choices=["strong", "weak"], default="strong",
+                   help="N > 1: strong = one batch cut into output-group shards (default); "
+                        "weak = a full-size batch per rank")
     p.add_argument("--scale", type=float, default=1.0,
                    help="shrink the number of outputs/entries (profiling runs only; not a bench value)")
     return p.parse_args()
@@ -75,13 +84,53 @@ def dist_env():
     return rank, world, local
 
 
-def make_batch(cfg: str, rank: int, scale: float = 1.0):
+def make_batch(cfg: str, rank: int, scale: float = 1.0, world: int = 1, scaling: str = "strong"):
+    """The rank's share of the workload.
+
+    strong (default): one seeded batch, cut into `world` shards at output-group
+    boundaries (sharding.shard_batch: entries sharing an output stay on one rank, so
+    no data crosses ranks); every rank builds the same batch and keeps its shard.
+    weak: every rank owns a full-size batch with its own seed."""
     from kronmult_gb300 import workloads as W
+    from kronmult_gb300.sharding import shard_batch
 
     fn, _ = CONFIGS[cfg]
-    # weak scaling: every rank owns a full-size shard with its own seed (shards are
-    # whole output groups, so no data crosses ranks)
-    return getattr(W, fn)(scale=scale, seed=getattr(W, fn).__defaults__[1] + 7919 * rank)
+    seed0 = getattr(W, fn).__defaults__[1]
+    if scaling == "weak" or world == 1:
+        b = getattr(W, fn)(scale=scale, seed=seed0 + (7919 * rank if scaling == "weak" else 0))
+        return b, b
+    full = getattr(W, fn)(scale=scale, seed=seed0)
+    shard, _ = shard_batch(full, rank, world)
+    return shard, full
+
+
+def config_dict(cfg: str, b, world: int, scaling: str = "strong") -> dict:
+    """The workload description (`b` = the whole job's batch), identical in both arms."""
+    _, wname = CONFIGS[cfg]
+    return {"workload": wname, "d": b.d, "n": b.n, "matrix_stride": b.stride, "nb_batch": b.nb,
+            "outputs": b.n_out, "fan_in": b.nb // max(b.n_out, 1),
+            "l2": "inputs (%.2f GB) larger than L2; no flush" % (b.inputs.nbytes / 1e9),
+            "parallelism": f"output-group shards x{world} ({scaling} scaling)"}
+
+
+def cpu_impl():
+    """The CPU implementation of the reference's algorithm to time: its own kronmult_omp,
+    built from its sources into oracle/_ref (rebuilt for this host's architecture from the
+    staged sources when needed).  Returns (impl, note); impl is "port" (the C restatement)
+    only when that build cannot be made here, and the note says why."""
+    from oracle import oracle as O
+
+    if not O.available("reference"):
+        try:
+            O.build(ref=True)
+        except Exception as exc:  # reported in the JSON line and on stderr
+            print(f"bench: building the reference kronmult_omp failed: {exc}", file=sys.stderr)
+    if O.available("reference"):
+        O.max_threads("reference")  # loads it: an unloadable build fails loudly here
+        return "reference", "the reference's kronmult_omp built from its sources (oracle/_ref)"
+    note = "reference kronmult_omp build missing on this host; timed the C restatement of it instead"
+    print(f"bench: {note}", file=sys.stderr)
+    return "port", note
 
 
 class ClockSampler:
@@ -137,71 +186,65 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(b, dtype, budget_s: float = 15.0):
-    """Time the oracle (OpenMP, all host threads) on the workload, or on a bounded
-    prefix of its entries when the whole would take longer than ~budget_s."""
-    from oracle import oracle as O
+def host_threads() -> int:
+    """Every host core this process may run on (a launcher may have set OMP_NUM_THREADS=1
+    for its ranks; the CPU legs run on rank 0 alone and use them all)."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def _prefix(b, count):
     from kronmult_gb300.workloads import Batch
 
-    try:
-        threads = len(os.sched_getaffinity(0))
-    except AttributeError:
-        threads = os.cpu_count() or 1
+    return Batch(b.name, b.d, b.n, b.stride, b.block, b.factors, b.inputs[:count], b.out_init,
+                 b.fac_index[:count], b.out_index[:count])
+
+
+def cpu_baseline(b, dtype, budget_s: float = 15.0):
+    """Time the reference's CPU implementation (cpu_impl: its own kronmult_omp, OpenMP,
+    all host threads) on the workload, or on a bounded prefix of its entries when the
+    whole would take longer than ~budget_s."""
+    from oracle import oracle as O
+
+    impl, note = cpu_impl()
+    threads = host_threads()
     probe = min(b.nb, 2048)
-    sub = Batch(b.name, b.d, b.n, b.stride, b.block, b.factors, b.inputs[:probe], b.out_init,
-                b.fac_index[:probe], b.out_index[:probe])
     t0 = time.perf_counter()
-    O.forward(sub, dtype=dtype, nthreads=threads)
-    t_probe = time.perf_counter() - t0
-    per_entry = t_probe / probe
+    O.forward(_prefix(b, probe), dtype=dtype, impl=impl, nthreads=threads)
+    per_entry = (time.perf_counter() - t0) / probe
     count = int(min(b.nb, max(probe, budget_s / 3 / max(per_entry, 1e-12))))
-    sub = Batch(b.name, b.d, b.n, b.stride, b.block, b.factors, b.inputs[:count], b.out_init,
-                b.fac_index[:count], b.out_index[:count])
+    sub = _prefix(b, count)
     best = float("inf")
     for _ in range(3):
         t0 = time.perf_counter()
-        O.forward(sub, dtype=dtype, nthreads=threads)
+        O.forward(sub, dtype=dtype, impl=impl, nthreads=threads)
         best = min(best, time.perf_counter() - t0)
     flops = 2.0 * b.d * b.n * b.N * count
-    return {"value": flops / best / 1e9, "unit": "GFLOP/s", "cores": threads, "kind": "port",
-            "sample": f"{count} of {b.nb} entries of the same batch, best of 3, {threads} OpenMP threads"}
+    return {"value": flops / best / 1e9, "unit": "GFLOP/s", "cores": threads, "kind": impl,
+            "sample": f"{count} of {b.nb} entries of the same batch, best of 3, {threads} OpenMP threads ({note})"}
 
 
 def run_reference(args, rank, world):
-    """--impl reference: the reference's CPU algorithm on the host cores."""
+    """--impl reference: the reference's own CPU implementation (kronmult_omp) on the host
+    cores, on this arm's workload, metric and config; rank 0 alone."""
     if rank != 0:
         return
-    b = make_batch(args.config, 0)
+    _, b = make_batch(args.config, 0, args.scale, world, args.scaling)
     dt = np.float64 if args.dtype == "f64" else np.float32
     from oracle import oracle as O
-    from kronmult_gb300.workloads import Batch
 
-    # every host core this process may run on (a launcher may have set OMP_NUM_THREADS=1
-    # for its ranks; the reference arm runs on rank 0 alone and uses them all)
-    try:
-        threads = len(os.sched_getaffinity(0))
-    except AttributeError:
-        threads = os.cpu_count() or 1
-    # the reference's own kronmult_omp when it was compiled here from its sources
-    # (oracle/_ref), else the C restatement of it
-    impl = "port"
-    if O.available("reference"):
-        try:
-            O.max_threads("reference")
-            impl = "reference"
-        except OSError:
-            impl = "port"
+    impl, note = cpu_impl()
+    threads = host_threads()
     # bounded sample per step so that warmup+steps stay within a few minutes
     probe = min(b.nb, 1024)
-    sub = Batch(b.name, b.d, b.n, b.stride, b.block, b.factors, b.inputs[:probe], b.out_init,
-                b.fac_index[:probe], b.out_index[:probe])
     t0 = time.perf_counter()
-    O.forward(sub, dtype=dt, impl=impl, nthreads=threads)
+    O.forward(_prefix(b, probe), dtype=dt, impl=impl, nthreads=threads)
     per_entry = (time.perf_counter() - t0) / probe
     total_steps = args.steps + args.warmup
     count = int(min(b.nb, max(64, 120.0 / total_steps / max(per_entry, 1e-12))))
-    sub = Batch(b.name, b.d, b.n, b.stride, b.block, b.factors, b.inputs[:count], b.out_init,
-                b.fac_index[:count], b.out_index[:count])
+    sub = _prefix(b, count)
     for _ in range(args.warmup):
         O.forward(sub, dtype=dt, impl=impl, nthreads=threads)
     t0 = time.perf_counter()
@@ -210,18 +253,14 @@ def run_reference(args, rank, world):
     el = time.perf_counter() - t0
     flops = 2.0 * b.d * b.n * b.N * count * args.steps
     v = flops / el / 1e9
-    _, wname = CONFIGS[args.config]
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "GFLOP/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.dtype,
+        "higher_is_better": True, "scaling": args.scaling, "vs_baseline": None, "dtype": args.dtype,
         "data": "synthetic (seeded PCG64; factors U[-1,1], inputs N(0,1))",
-        "config": {"workload": wname, "d": b.d, "n": b.n, "matrix_stride": b.stride, "nb_batch": b.nb,
-                   "outputs": b.n_out, "sample_entries_per_step": count},
+        "config": config_dict(args.config, b, world, args.scaling),
         "cpu_baseline": {"value": v, "unit": "GFLOP/s", "cores": threads, "kind": impl,
-                         "sample": f"{count} of {b.nb} entries per step, {threads} OpenMP threads " + (
-                             "(the reference's kronmult_omp built from its sources)" if impl == "reference" else
-                             "(C restatement of kronmult_omp; the reference build is not on this host)")},
+                         "sample": f"{count} of {b.nb} entries per step, {threads} OpenMP threads ({note})"},
         "e2e": {"value": v, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -356,7 +395,7 @@ def suite(args):
 
     import torch
 
-    from kronmult_gb300 import DeviceBatch, _lib, adjoint, forward_f32_f64out
+    from kronmult_gb300 import DeviceBatch, _lib, adjoint, check_device_error, forward_f32_f64out
     from kronmult_gb300 import grouped as G
     from kronmult_gb300 import workloads as W
     from oracle import oracle as O
@@ -488,6 +527,7 @@ def suite(args):
             db.outputs.zero_()
             forward_f32_f64out(db, compute=code, stream=st)
         torch.cuda.synchronize()
+        check_device_error()  # a tensor-core wait that ran out would leave incomplete outputs
         got = db.outputs.cpu().numpy()
         emit(f"c4_fwd_{cname}", b, ms, 4, 8, {"rel_l2_vs_fp64": O.rel_l2(got, ref), "max_err_vs_fp64": O.max_rel(got, ref)})
     del db
@@ -571,13 +611,15 @@ def main():
     from kronmult_gb300 import DeviceBatch, _lib
 
     lib = _lib.lib()
-    b = make_batch(args.config, rank, args.scale)
+    b, full = make_batch(args.config, rank, args.scale, world, args.scaling)
     tdt = torch.float64 if args.dtype == "f64" else torch.float32
     esize = 8 if args.dtype == "f64" else 4
     db = DeviceBatch.from_host(b, device=dev, dtype=tdt)
     stream = torch.cuda.Stream(dev)
-    flops_step = b.flops()
+    flops_step = b.flops()  # this rank's shard
     bytes_step = b.bytes(in_size=esize, out_size=esize)
+    # the whole job per step: every rank's shard (strong), or world full batches (weak)
+    job_flops = full.flops() * (world if args.scaling == "weak" else 1)
 
     def barrier():
         if world > 1:
@@ -607,7 +649,7 @@ def main():
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = t.item()
     per_launch_s = ms / 1e3 / args.steps
-    value = flops_step * world / per_launch_s / 1e9
+    value = job_flops / per_launch_s / 1e9
 
     # ---- end to end through the public API with pinned host buffers
     h_in = torch.from_numpy(b.inputs).to(tdt).pin_memory()
@@ -644,7 +686,7 @@ def main():
         return ms
 
     e2e_ms = time_host_steps(e2e_step)
-    e2e_value = flops_step * world / (e2e_ms / 1e3) / 1e9
+    e2e_value = job_flops / (e2e_ms / 1e3) / 1e9
     e2e_mapped_ms = None
     if tdt == torch.float64 and h_in.shape == db.inputs.shape and h_fac.shape == db.factors.shape:
         e2e_mapped_ms = time_host_steps(e2e_mapped_step)
@@ -701,16 +743,12 @@ def main():
         cpu = cpu_baseline(b, np.float64 if args.dtype == "f64" else np.float32)
 
     if rank == 0:
-        _, wname = CONFIGS[args.config]
         line = {
             "metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": args.dtype,
+            "scaling": args.scaling, "vs_baseline": None, "dtype": args.dtype,
             "data": "synthetic (seeded PCG64; factors U[-1,1], inputs N(0,1))",
-            "config": {"workload": wname, "d": b.d, "n": b.n, "matrix_stride": b.stride, "nb_batch": b.nb,
-                       "outputs": b.n_out, "fan_in": b.nb // max(b.n_out, 1),
-                       "l2": "inputs (%.2f GB) larger than L2; no flush" % (b.inputs.nbytes / 1e9),
-                       "parallelism": f"output-group shards x{world}"},
+            "config": config_dict(args.config, full, world, args.scaling),
             "gbytes_per_s": achieved_gbs,
             "roofline": roofline,
             "cpu_baseline": cpu,
@@ -719,7 +757,7 @@ def main():
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
                     "path": "api.forward_from_host: staging copies from pinned host memory, 12 pieces",
                     "mapped_inputs": None if e2e_mapped_ms is None else {
-                        "ms_per_step": e2e_mapped_ms, "value": flops_step * world / (e2e_mapped_ms / 1e3) / 1e9,
+                        "ms_per_step": e2e_mapped_ms, "value": job_flops / (e2e_mapped_ms / 1e3) / 1e9,
                         "path": "api.forward_from_host_mapped: kernels read inputs and factors from pinned "
                                 "host memory over the CPU-GPU link, outputs copied back"}},
             "gpu_launches": args.steps,

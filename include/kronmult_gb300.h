@@ -182,15 +182,23 @@ int kronmult_tuning_cache_load(const char *path);
  *
  * Same result as kronmult_batched_f64 (output[k] += kron(A_k) . input[k], atomic
  * into shared outputs); inputs are not modified; every pointer array on the
- * device.  Each run of consecutive entries with one output pointer is summed in
+ * device.  Work is handed out in pieces: a run of consecutive entries with one
+ * output pointer, cut at entry indices that are multiples of 16 once the run holds
+ * more than 16 entries, so that a few long runs (thousands of entries into a
+ * handful of outputs) still spread over the whole GPU.  Each piece is summed in
  * entry order and added with one atomic per element, so the result is bitwise
- * reproducible when every output's entries form one contiguous run.
- * Limits: nb_batch <= KRONMULT_NOALLOC_MAX_ENTRIES (else cudaErrorInvalidValue),
- * 2 <= matrix_size <= 8 with n^d fitting one team's shared memory (else
- * cudaErrorNotSupported).  The first call on a device looks up the array's
- * device address (cudaGetSymbolAddress) with that device current; make that first
- * call before any stream capture.  All calls share the array: calls that overlap
- * on the GPU (other streams, other host threads) race and must be serialised.
+ * reproducible when every output's entries form one contiguous run of at most 16
+ * entries.
+ * Limits: nb_batch <= KRONMULT_NOALLOC_MAX_ENTRIES (else cudaErrorInvalidValue);
+ * 2 <= matrix_size <= 8, n^(d-1) <= 1024 (at most 4 fibres per thread of a
+ * 256-thread team) and n^d fitting one team's shared memory (else
+ * cudaErrorNotSupported; e.g. n = 2, d = 12 is refused).  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress) with that
+ * device current, under a lock, and keeps it for the process: make that first call
+ * before any stream capture, and do not call this entry point on a device after
+ * cudaDeviceReset.  All calls share the array and it keeps the last call's contents
+ * (its counters are cleared at the start of every call): calls that overlap on the
+ * GPU (other streams, other host threads) race and must be serialised.
  */
 #define KRONMULT_NOALLOC_MAX_ENTRIES 1048576
 int kronmult_batched_f64_noalloc(int matrix_count, int matrix_size, const double *const *matrix_list_batched,

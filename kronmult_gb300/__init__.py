@@ -7,11 +7,12 @@ runs in the hand-written CUDA library libkronmult_gb300.so behind a C ABI
 """
 from ._lib import (KRONMULT_COMPUTE_BF16, KRONMULT_COMPUTE_FP32, KRONMULT_COMPUTE_TF32, KronmultError,
                    Tuning, lib)
-from .api import DeviceBatch, adjoint, forward_f32_f64out, kronmult_batched, kronmult_batched_async
+from .api import (DeviceBatch, adjoint, check_device_error, forward_f32_f64out, kronmult_batched,
+                  kronmult_batched_async)
 from .workloads import Batch, make_batch
 
 __all__ = [
     "Batch", "DeviceBatch", "adjoint", "KronmultError", "Tuning", "lib", "make_batch", "kronmult_batched",
-    "kronmult_batched_async", "forward_f32_f64out", "KRONMULT_COMPUTE_FP32", "KRONMULT_COMPUTE_TF32",
+    "kronmult_batched_async", "forward_f32_f64out", "check_device_error", "KRONMULT_COMPUTE_FP32", "KRONMULT_COMPUTE_TF32",
     "KRONMULT_COMPUTE_BF16",
 ]

@@ -42,9 +42,9 @@ KRONMULT_NOALLOC_MAX_ENTRIES = 1048576
 class KronmultError(RuntimeError):
     """A non-zero status (a cudaError_t value) returned by the library."""
 
-    def __init__(self, status: int, where: str):
+    def __init__(self, status: int, where: str, detail: str | None = None):
         self.status = status
-        super().__init__(f"{where} failed with status {status}: {error_string(status)}")
+        super().__init__(f"{where} failed with status {status}: {detail or error_string(status)}")
 
 
 _lock = threading.Lock()

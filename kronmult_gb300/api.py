@@ -132,9 +132,7 @@ class DeviceBatch:
                 kronmult_batched_async(self.d, self.n, self.mat_ptrs, self.stride, self.in_ptrs, self.out_ptrs,
                                        self.ws_ptrs, self.nb, dtype=dt, stream=stream, tuning=tuning)
         elif dt == torch.float32 and self.outputs.dtype == torch.float64:
-            forward_f32_f64out(self, compute=_lib.KRONMULT_COMPUTE_FP32, stream=stream, tuning=tuning)
-            if sync:
-                torch.cuda.synchronize()
+            forward_f32_f64out(self, compute=_lib.KRONMULT_COMPUTE_FP32, stream=stream, tuning=tuning, sync=sync)
         else:
             raise TypeError(f"unsupported storage/output dtypes {dt}/{self.outputs.dtype}")
 
@@ -193,14 +191,33 @@ def adjoint(b: DeviceBatch, grad_outputs: torch.Tensor, grad_inputs: torch.Tenso
     b._adj_keep = gout
 
 
+def check_device_error(clear: bool = True) -> None:
+    """Raise KronmultError when a tensor-core kernel recorded a device-side failure (a
+    bounded mbarrier wait that ran out: the kernel left early and its outputs are
+    incomplete).  Reads the library's device error word (kronmult_device_error), which
+    waits for the work already enqueued; with `clear` the word is reset."""
+    code = ctypes.c_int(0)
+    _lib.check(_lib.lib().kronmult_device_error(ctypes.byref(code), int(clear)), "kronmult_device_error")
+    if code.value:
+        raise _lib.KronmultError(code.value, "a tensor-core kernel",
+                                 "device error word set: a bounded mbarrier wait timed out and the kernel "
+                                 "left early, so its outputs are incomplete")
+
+
 def forward_f32_f64out(b: DeviceBatch, compute: int = _lib.KRONMULT_COMPUTE_FP32, stream=None,
-                       tuning=None) -> None:
-    """FP32 factors/inputs, FP32 (or TF32/BF16 tensor-core) contraction, FP64 output accumulation."""
+                       tuning=None, sync: bool = False) -> None:
+    """FP32 factors/inputs, FP32 (or TF32/BF16 tensor-core) contraction, FP64 output accumulation.
+    Enqueues only, unless `sync`: then it waits for the stream and, for the tensor-core
+    modes, raises if the kernel recorded a device-side failure (check_device_error)."""
     fn = _lib.lib().kronmult_batched_f32_f64out_async
     st = fn(b.d, b.n, b.mat_ptrs.data_ptr(), b.stride, b.in_ptrs.data_ptr(), b.out_ptrs.data_ptr(),
             None if b.ws_ptrs is None else b.ws_ptrs.data_ptr(), b.nb, int(compute), _stream_handle(stream),
             _lib.tuning_ptr(tuning))
     _lib.check(st, "kronmult_batched_f32_f64out_async")
+    if sync:
+        torch.cuda.synchronize()
+        if compute != _lib.KRONMULT_COMPUTE_FP32:
+            check_device_error()
 
 
 def forward_from_host(b: DeviceBatch, h_inputs: torch.Tensor, h_factors: torch.Tensor, h_outputs: torch.Tensor,

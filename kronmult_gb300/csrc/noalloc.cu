@@ -10,12 +10,16 @@
 //
 // What it computes: the same as kronmult_batched_f64 (output[k] += kron(A_k).input[k],
 // atomic into shared outputs).  Work is scheduled by output run, as in the
-// deterministic grouped mode: a first kernel lists the start of every run of
-// consecutive entries with the same output pointer; a persistent kernel hands the
-// runs to teams through a queue counter; each team sums its run in entry order and
-// adds the sum with one atomic per element.  When every output's entries are one
-// contiguous run, each output element receives exactly one addition and the
-// result is bitwise reproducible.
+// deterministic grouped mode: a first kernel lists the start of every piece of work,
+// a persistent kernel hands the pieces to teams through a queue counter, and each
+// team sums its piece in entry order and adds the sum with one atomic per element.
+// A piece is a run of consecutive entries with the same output pointer, cut where
+// the entry index is a multiple of kNaPiece (16) and the run already holds more than
+// 16 entries, so that one long run (the reference's benchmarks send thousands of
+// entries into 5 outputs) is spread over many teams instead of serialising on one.
+// When every output's entries are one contiguous run of at most 16 entries, each
+// output element receives exactly one addition and the result is bitwise
+// reproducible.
 //
 // Scratch: g_noalloc_scratch below, 4 MiB + 256 bytes, holding two counters and
 // up to KRONMULT_NOALLOC_MAX_ENTRIES run starts.  Every GPU that loads the library
@@ -24,6 +28,7 @@
 // Calls that overlap on the GPU (concurrent streams, or several host threads)
 // race on the array and must be serialised by the caller.
 #include <climits>
+#include <mutex>
 #include "fwd_kernels.cuh"
 #include "kronmult_gb300.h"
 
@@ -34,6 +39,18 @@ namespace kgb {
 namespace {
 
 constexpr int kNaBlock = 256;
+constexpr int kNaPiece = 16;  // longest piece of a long run that one team sums before its atomics
+
+// Entry k starts a piece: it is the first entry, its output differs from entry k-1's, or
+// k is a multiple of kNaPiece and entry k-kNaPiece adds into the same output (so the run
+// around k is longer than kNaPiece).  Runs of at most kNaPiece entries are never cut.
+__device__ __forceinline__ bool piece_start(double *const *out, int k)
+{
+    if (k == 0) return true;
+    const double *o = out[k];
+    if (out[k - 1] != o) return true;
+    return (k % kNaPiece) == 0 && out[k - kNaPiece] == o;
+}
 
 struct NaArgs {
     const double *const *mats;
@@ -44,11 +61,11 @@ struct NaArgs {
     int nb, d, stride, N, team_size, team_elems, vec_pad;
 };
 
-// run starts: entry k starts a run when it is first or its output differs from entry k-1's
+// piece starts, in no particular order
 __global__ void noalloc_runs_kernel(const NaArgs a)
 {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < a.nb; k += gridDim.x * blockDim.x) {
-        if (k == 0 || a.out[k] != a.out[k - 1]) {
+        if (piece_start(a.out, k)) {
             const unsigned slot = atomicAdd(&a.counters[0], 1u);
             a.runs[slot] = k;
         }
@@ -71,9 +88,8 @@ template <int NN, int QMAX> __global__ void __launch_bounds__(kNaBlock) noalloc_
         const int start = s_run[tm.id];
         tm.sync();
         if (start < 0) break;
-        double *o = a.out[start];
         int end = start + 1;
-        while (end < a.nb && a.out[end] == o) ++end;
+        while (end < a.nb && !piece_start(a.out, end)) ++end;
         team_forward<double, double, NN, QMAX, false>(a.mats, a.in, a.out, nullptr, a.d, a.stride, a.N, start, end,
                                                       buf, buf + a.vec_pad, tm);
     }
@@ -99,17 +115,26 @@ NaFn noalloc_lookup(int nn, int qmax)
 }
 
 // Device address of the scratch array, looked up once per device with that device
-// current.  Fixed-size table: no allocation.
+// current (host code cannot use the array's name as a device address).  Fixed-size
+// table, filled under a lock so that concurrent first calls from several host threads
+// are safe.  No allocation.  The address belongs to the device's current context: after
+// cudaDeviceReset the cached value would be stale, so a process that resets a device
+// must not call this entry point on it again.
 constexpr int kMaxDevices = 64;
 void *g_scratch_ptr[kMaxDevices] = {};
+std::mutex g_scratch_mutex;
 
 int scratch_address(int dev, void **out)
 {
     if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
     if (g_scratch_ptr[dev] == nullptr) {
         void *p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return e;
+        if (e != cudaSuccess) {
+            cudaGetLastError();  // leave no sticky status behind for later, unrelated calls
+            return e;
+        }
         g_scratch_ptr[dev] = p;
     }
     *out = g_scratch_ptr[dev];
@@ -164,10 +189,15 @@ extern "C" int kronmult_batched_f64_noalloc(int matrix_count, int matrix_size,
     if (smem + 256 > (size_t)smem_optin) return cudaErrorNotSupported;  // 256 B kept for the static run slots
     const NaFn fn = noalloc_lookup(n, qmax);
     if (!fn) return cudaErrorNotSupported;
-    if ((e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
+    if ((e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess) {
+        cudaGetLastError();  // clear it: the status is returned here, not left for a later call
         return e;
+    }
     int per_sm = 0;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, teams * ts, smem)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, teams * ts, smem)) != cudaSuccess) {
+        cudaGetLastError();
+        return e;
+    }
     if (per_sm < 1) per_sm = 1;
 
     NaArgs a{};
@@ -185,7 +215,10 @@ extern "C" int kronmult_batched_f64_noalloc(int matrix_count, int matrix_size,
     a.vec_pad = vpad;
 
     cudaStream_t st = (cudaStream_t)stream;
-    if ((e = cudaMemsetAsync(scratch, 0, 2 * sizeof(unsigned), st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(scratch, 0, 2 * sizeof(unsigned), st)) != cudaSuccess) {
+        cudaGetLastError();
+        return e;
+    }
     const int grid_runs = (nb_batch + 255) / 256 < sms * 4 ? (nb_batch + 255) / 256 : sms * 4;
     noalloc_runs_kernel<<<grid_runs, 256, 0, st>>>(a);
     fn<<<sms * per_sm, teams * ts, smem, st>>>(a);

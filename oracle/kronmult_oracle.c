@@ -8,8 +8,8 @@
  * It is a plain-C restatement of the reference's CPU path (kronmult_omp):
  *   - kronmult_batched   kronmult_omp/kronmult.hpp:77-104  (OpenMP over entries)
  *   - kronmult           kronmult_omp/kronmult.hpp:32-60   (backward Algorithm-993 sweep)
- *   - multiply_transpose kronmult_omp/linear_algebra.hpp:206-225 (loop variant, no BLAS)
- *   - transpose          kronmult_omp/linear_algebra.hpp:182-192
+ *   - multiply_transpose kronmult_omp/linear_algebra.hpp:102-121 (loop variant, no BLAS)
+ *   - transpose          kronmult_omp/linear_algebra.hpp:78-88
  * and of the reference's naive explicit-Kronecker check
  *   - kronmult_naive     tests/utils/kronmult_naive.h:73-102
  *   - kronecker_product  tests/utils/kronmult_naive.h:47-67
@@ -50,7 +50,7 @@ static int64_t ipow64(int64_t b, int e)
 
 #define DEFINE_ORACLE(T, SUF)                                                                            \
     /* Mt = M^T with leading dimension n; M has leading dimension `stride`                            \
-     * (kronmult_omp/linear_algebra.hpp:182-192) */                                                   \
+     * (kronmult_omp/linear_algebra.hpp:78-88) */                                                   \
     static void transpose_##SUF(const T *M, T *Mt, int n, int stride)                                  \
     {                                                                                                  \
         for (int r = 0; r < n; r++)                                                                    \
@@ -58,7 +58,7 @@ static int64_t ipow64(int64_t b, int e)
     }                                                                                                  \
                                                                                                        \
     /* Y = X^T M^T, X is n x ncol (ld n), Y is ncol x n (ld ncol)                                      \
-     * (kronmult_omp/linear_algebra.hpp:206-225) */                                                   \
+     * (kronmult_omp/linear_algebra.hpp:102-121) */                                                   \
     static void multiply_transpose_##SUF(const T *X, int64_t ncol, const T *M, int n, int stride, T *Y, \
                                          T *Mt)                                                        \
     {                                                                                                  \

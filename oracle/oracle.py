@@ -6,7 +6,7 @@ CPU-baseline / reference legs, never by the kronmult_gb300 package.
 Three implementations of the same maths, all on host arrays of a
 `kronmult_gb300.workloads.Batch`:
   port       liboracle.so, the C restatement in kronmult_oracle.c
-             (kronmult_omp/kronmult.hpp:77-104 and linear_algebra.hpp:182-225)
+             (kronmult_omp/kronmult.hpp:32-104 and linear_algebra.hpp:78-121)
   reference  _ref/libkronmult_omp_ref.so, the reference's own kronmult_omp built from
              its sources by oracle/Makefile (only where those sources exist)
   naive      the explicit-Kronecker check of tests/utils/kronmult_naive.h:73-121,
@@ -63,6 +63,7 @@ def _load(kind: str) -> ctypes.CDLL:
             f = getattr(h, f"ref_kronmult_naive_{suf}")
             f.restype, f.argtypes = i, [i, i, vp, i, vp, vp, i]
         h.ref_max_threads.restype = i
+        h.ref_set_num_threads.restype, h.ref_set_num_threads.argtypes = None, [i]
     _libs[key] = h
     return h
 
@@ -134,7 +135,7 @@ def _call(impl, suf, b, mats, ins, outp, inputs, nthreads):
         ins2 = np.uint64(icopy.ctypes.data) + k * np.uint64(icopy.shape[1] * icopy.itemsize)
         wsp = np.uint64(ws.ctypes.data) + k * np.uint64(ws.shape[1] * ws.itemsize)
         if nthreads:
-            os.environ["OMP_NUM_THREADS"] = str(nthreads)
+            h.ref_set_num_threads(int(nthreads))
         rc = getattr(h, f"ref_kronmult_batched_{suf}")(b.d, b.n, mats.ctypes.data, b.stride, ins2.ctypes.data,
                                                        outp.ctypes.data, wsp.ctypes.data, b.nb)
     elif impl == "naive":
@@ -153,6 +154,60 @@ def _call(impl, suf, b, mats, ins, outp, inputs, nthreads):
         raise ValueError(f"unknown oracle implementation {impl!r}")
     if rc != 0:
         raise RuntimeError(f"oracle {impl} failed with status {rc}")
+
+
+def factor_matrices(b, dtype=np.float64) -> np.ndarray:
+    """Every factor row of the batch as an (rows, n, n) array of n x n matrices
+    (row r, column c at offset r + c*stride of the col-major storage)."""
+    n, st = b.n, b.stride
+    F = np.asarray(b.factors, dtype=dtype)[:, :n * st].reshape(-1, n, st)[:, :, :n]  # [row, c, r]
+    return np.ascontiguousarray(F.transpose(0, 2, 1))
+
+
+def transposed_batch(b, grad_out):
+    """The batch whose forward is the adjoint's grad_input: factors A^T (stride n), each
+    entry's input the gradient of the output it adds into, one output per entry.  The
+    adjoint of kronmult_batched is the reference applied with transposed factors
+    (kronmult_omp/kronmult.hpp:77-104 on A_i^T)."""
+    from kronmult_gb300.workloads import Batch
+
+    n = b.n
+    At = factor_matrices(b).transpose(0, 2, 1)  # A^T per row
+    fac_t = np.ascontiguousarray(At.transpose(0, 2, 1)).reshape(-1, n * n)  # col-major, ld n
+    return Batch(b.name + "_T", b.d, n, n, n * n, fac_t, np.asarray(grad_out)[b.out_index],
+                 np.zeros((b.nb, b.N)), b.fac_index, np.arange(b.nb, dtype=np.int64))
+
+
+def _apply_mode(T, A, axis):
+    """T (B, n, ..., n) with the batch's matrices A (B, n, n) applied along tensor axis `axis`."""
+    Tm = np.moveaxis(T, axis + 1, -1)
+    sh = Tm.shape
+    R = np.matmul(Tm.reshape(sh[0], -1, sh[-1]), A.transpose(0, 2, 1)).reshape(sh)
+    return np.moveaxis(R, -1, axis + 1)
+
+
+def grad_factors(b, grad_out, dtype=np.float64) -> np.ndarray:
+    """dL/dA for L = sum_e <grad_out[e], out[e]>, as (rows, n, n) matrices summed over the
+    entries sharing a factor row.  Mode-unfolding formula: for entry k and mode i,
+    dL/dA_{k,i} = G_(i) . U_(i)^T, with G the gradient of entry k's output as an n^d tensor
+    (A_0 the most significant index) and U the input with every factor but A_i applied.
+    The reference has no gradient; this formula is checked against central finite
+    differences of the forward in the tests."""
+    n, d = b.n, b.d
+    A = factor_matrices(b, dtype)
+    rows = A.shape[0]
+    X = np.asarray(b.inputs, dtype=dtype).reshape((b.nb,) + (n,) * d)
+    G = np.asarray(grad_out, dtype=dtype)[b.out_index].reshape((b.nb,) + (n,) * d)
+    out = np.zeros((rows, n, n), dtype=dtype)
+    for i in range(d):
+        U = X
+        for m in range(d):
+            if m != i:
+                U = _apply_mode(U, A[b.fac_index * d + m], m)
+        Gi = np.moveaxis(G, i + 1, 1).reshape(b.nb, n, -1)
+        Ui = np.moveaxis(U, i + 1, 1).reshape(b.nb, n, -1)
+        np.add.at(out, b.fac_index * d + i, np.matmul(Gi, Ui.transpose(0, 2, 1)))
+    return out
 
 
 def rel_l2(a, b) -> float:

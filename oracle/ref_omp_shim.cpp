@@ -52,6 +52,18 @@ int ref_kronmult_naive_f32(int d, int n, float **mats, int stride, float **in, f
     return 0;
 }
 
+/* Sets the OpenMP team size of later calls (OMP_NUM_THREADS is read only when the
+ * OpenMP runtime loads, so a launcher's OMP_NUM_THREADS=1 cannot be undone through
+ * the environment afterwards). */
+void ref_set_num_threads(int n)
+{
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
 int ref_max_threads(void)
 {
 #ifdef _OPENMP

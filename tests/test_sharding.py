@@ -78,3 +78,26 @@ def test_two_rank_gloo_shards():
         assert p.exitcode == 0
     assert err <= 1e-15
     assert all(m == 1.0 for m in mask)  # every output owned by exactly one rank
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("world", [2, 3])
+def test_shards_through_cuda_union_equals_oracle(cuda, world):
+    """The shards bench.py gives each rank (sharding.shard_batch of one seeded batch),
+    run one after another through the CUDA forward on one GPU: every output is
+    computed by exactly one shard, and the union equals the oracle on the whole batch."""
+    import torch
+
+    from kronmult_gb300 import DeviceBatch
+    from oracle import oracle as O
+
+    b = W.config3(scale=0.05)[2]  # d=4, n=4, ragged fan-in 1..27
+    full = np.full((b.n_out, b.N), np.nan)
+    for r in range(world):
+        shard, outs = shard_batch(b, r, world)
+        db = DeviceBatch.from_host(shard, device=cuda)
+        db.forward(sync=True)
+        assert np.all(np.isnan(full[outs])), "an output computed by two shards"
+        full[outs] = db.outputs.cpu().numpy()
+    assert not np.isnan(full).any()
+    assert O.rel_l2(full, O.forward(b)) <= 1e-13
