@@ -16,6 +16,18 @@
 // the mode output straight into the next mode's operand layout at the rotated
 // positions, so the vector never leaves shared memory.
 //
+// BF16 (fwd_tc_bf16_kernel) keeps the vector operand MN-major (8 consecutive fibres =
+// 16 contiguous bytes per K row of a core matrix) and applies the modes in the order
+// 0, 1, ..., d-1: the contracted index is then always the most significant digit of the
+// fibre index, and the 8 outputs a thread reads from its TMEM lane (one fibre, the 8
+// values of the new index) are 8 consecutive fibres of the next mode's operand, written
+// with ONE 16-byte store.  The first operand is the natural vector itself read as
+// MN-major (fibre = the fastest d-1 indices, K = the slowest), converted 8 values per
+// 16-byte store.  Two 128-fibre tiles share one MMA: K = 16 holds the even tile in K
+// rows 0..7 and the odd one in rows 8..15, against the block-diagonal factor operand
+// [A_i 0; 0 A_i], so the operand carries no zero padding.  TF32 (fwd_tc_kernel; K = 8
+// per MMA) keeps the backward order and the K-major operand, written element by element.
+//
 // One CTA = one warpgroup (128 threads) works on one entry at a time; several
 // CTAs per SM overlap the input loads.  Consecutive entries with the same
 // output pointer are summed in tensor memory and added with FP64 atomics.
@@ -38,6 +50,11 @@ constexpr int kTileRows = 128;               // fibres per MMA (M)
 constexpr int kTileBytes = kTileRows * 32;   // one K-major tile: 128 rows x 32 bytes
 constexpr int kBBytes = 16 * 32;             // one factor operand: 16 rows x 32 bytes
 constexpr unsigned kWaitLimit = 1u << 22;    // bounded mbarrier polling
+// BF16 MN-major vector operand: per group of 8 fibres, K rows 0..7 (128 bytes), K rows
+// 8..15 (128 bytes), then 16 bytes of padding, so that 8 consecutive groups start in 8
+// different 16-byte bank slots
+constexpr uint32_t kMnLbo = 128;                 // K-group stride
+constexpr uint32_t kMnSbo = 272;                 // 8-fibre group stride
 
 enum : int { KIND_TF32 = 0, KIND_BF16 = 1 };
 
@@ -76,11 +93,12 @@ __device__ __forceinline__ uint32_t a_offset(uint32_t row, uint32_t kbyte, uint3
     return (row >> 3) * 128u + (kbyte >> 4) * lbo + (row & 7u) * 16u + (kbyte & 15u);
 }
 
-template <int KIND> __device__ __forceinline__ constexpr uint32_t instr_desc()
+template <int KIND, bool A_MN_MAJOR = false> __device__ __forceinline__ constexpr uint32_t instr_desc()
 {
-    // D = F32; A, B = TF32 (2) or BF16 (1); both K-major; N = 16; M = 128
+    // D = F32; A, B = TF32 (2) or BF16 (1); A K-major, or MN-major (bit 15, "transpose A");
+    // B K-major; N = 16; M = 128
     return (1u << 4) | ((KIND == KIND_TF32 ? 2u : 1u) << 7) | ((KIND == KIND_TF32 ? 2u : 1u) << 10) |
-           ((16u >> 3) << 17) | ((128u >> 4) << 24);
+           ((A_MN_MAJOR ? 1u : 0u) << 15) | ((16u >> 3) << 17) | ((128u >> 4) << 24);
 }
 
 template <int KIND>
@@ -96,6 +114,70 @@ __device__ __forceinline__ void mma(uint32_t dtmem, uint64_t adesc, uint64_t bde
             "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
             "l"(adesc), "l"(bdesc), "r"(instr_desc<KIND>()), "r"(accumulate));
+    }
+}
+
+// BF16 MMA with an MN-major A operand (the vector) and a K-major B operand (the factor)
+__device__ __forceinline__ void mma_bf16_mn(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
+        "l"(adesc), "l"(bdesc), "r"(instr_desc<KIND_BF16, true>()), "r"(accumulate));
+}
+
+// 8 FP32 values rounded to BF16 (nearest even), packed in order into 16 bytes
+__device__ __forceinline__ uint4 pack_bf16x8(float a0, float a1, float a2, float a3, float a4, float a5, float a6,
+                                             float a7)
+{
+    uint4 r;
+    __nv_bfloat162 h;
+    h = __floats2bfloat162_rn(a0, a1);
+    r.x = *reinterpret_cast<uint32_t *>(&h);
+    h = __floats2bfloat162_rn(a2, a3);
+    r.y = *reinterpret_cast<uint32_t *>(&h);
+    h = __floats2bfloat162_rn(a4, a5);
+    r.z = *reinterpret_cast<uint32_t *>(&h);
+    h = __floats2bfloat162_rn(a6, a7);
+    r.w = *reinterpret_cast<uint32_t *>(&h);
+    return r;
+}
+
+// BF16 K-stacked operand: the tiles of a pair (128 fibres each) share 8-fibre groups; K
+// rows 0..7 of a group hold the even tile, K rows 8..15 (one K-group = 128 bytes later)
+// the odd one, so one MMA with K = 16 and a block-diagonal factor operand computes both
+// tiles and no operand byte is padding.  Byte offset of fibre group g, K row kk:
+constexpr uint32_t kPairBytes = 16 * kMnSbo;  // 16 groups of 8 fibres
+constexpr int kBf16B = 512;                   // factor operand: 16 rows x 16 K x 2 bytes
+__device__ __forceinline__ uint32_t mn_offset(uint32_t g, uint32_t kk)
+{
+    const uint32_t t = g >> 4;  // tile of the group
+    return (t >> 1) * kPairBytes + (g & 15u) * kMnSbo + (t & 1u) * kMnLbo + kk * 16u;
+}
+
+// FP64 addition into global memory without a returned value
+__device__ __forceinline__ void red_add_f64(double *p, double v)
+{
+    asm volatile("red.global.add.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
+}
+
+// 8x8 transpose across the 8 lanes of each aligned lane octet: afterwards lane l's v[j]
+// is lane j's former v[l] (three butterfly stages of register-pair exchanges)
+__device__ __forceinline__ void octet_transpose(float (&v)[8], int lane)
+{
+#pragma unroll
+    for (int s = 4; s >= 1; s >>= 1) {
+        const bool upper = (lane & s) != 0;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            if (j & s) continue;
+            const float send = upper ? v[j] : v[j | s];
+            const float recv = __shfl_xor_sync(0xffffffffu, send, s);
+            if (upper)
+                v[j] = recv;
+            else
+                v[j | s] = recv;
+        }
     }
 }
 
@@ -288,7 +370,7 @@ template <int KIND> __global__ void __launch_bounds__(kTcThreads, 6) fwd_tc_kern
             const int c = t * kTileRows + warp * 32 + lane;
             if (t < a.tiles && c < F)
 #pragma unroll
-                for (int r = 0; r < 8; ++r) atomicAdd(dst + c + r * F, (double)v[r]);
+                for (int r = 0; r < 8; ++r) red_add_f64(dst + c + r * F, (double)v[r]);
         };
 #pragma unroll
         for (int j = 0; j < MAXT / 2; ++j) {
@@ -324,13 +406,13 @@ template <int KIND> __global__ void __launch_bounds__(kTcThreads, 6) fwd_tc_kern
                 put<KIND>(bs2 + (size_t)i * kBBytes, r + 8, k, fv[s]);
             }
         }
+        // natural position p = k + 8c -> operand row c, column k: the 4 values of a float4
+        // are one 16-byte half of a core-matrix row
         for (int q = tid; q < N / 4; q += kTcThreads) {
             const float4 v4 = *reinterpret_cast<const float4 *>(raw + 4 * q);
-            const uint32_t c = q >> 1, k0 = (q & 1) * 4;
-            put<KIND>(xs, c, k0 + 0, v4.x, lboa);
-            put<KIND>(xs, c, k0 + 1, v4.y, lboa);
-            put<KIND>(xs, c, k0 + 2, v4.z, lboa);
-            put<KIND>(xs, c, k0 + 3, v4.w, lboa);
+            const uint32_t c = q >> 1, kbyte = (q & 1) * 16;
+            *reinterpret_cast<float4 *>(xs + a_offset(c, kbyte, lboa)) =
+                make_float4(to_tf32(v4.x), to_tf32(v4.y), to_tf32(v4.z), to_tf32(v4.w));
         }
         // the run continues when this entry adds into the same output as the previous one;
         // otherwise the previous run's sum leaves TMEM before the last mode overwrites it
@@ -374,10 +456,19 @@ template <int KIND> __global__ void __launch_bounds__(kTcThreads, 6) fwd_tc_kern
                 auto store_tile = [&](int t, const float (&v)[8]) {
                     const int c = t * kTileRows + warp * 32 + lane;
                     if (t < a.tiles && c < F) {
+                        if (F >= 64) {
+                            // F/8 a multiple of 8: row p/8 = c/8 + r*F/8 keeps its position in
+                            // the 8-row group and moves r*F/64 groups, 2F bytes per r
+                            const uint32_t base = a_offset((uint32_t)c >> 3, 4u * ((uint32_t)c & 7u), lboa);
 #pragma unroll
-                        for (int r = 0; r < 8; ++r) {
-                            const uint32_t p = c + r * F;
-                            put<KIND>(xs, p >> 3, p & 7, v[r], lboa);
+                            for (int r = 0; r < 8; ++r)
+                                *reinterpret_cast<float *>(xs + base + (uint32_t)r * 2u * (uint32_t)F) = to_tf32(v[r]);
+                        } else {
+#pragma unroll
+                            for (int r = 0; r < 8; ++r) {
+                                const uint32_t p = c + r * F;
+                                put<KIND>(xs, p >> 3, p & 7, v[r], lboa);
+                            }
                         }
                     }
                 };
@@ -389,6 +480,215 @@ template <int KIND> __global__ void __launch_bounds__(kTcThreads, 6) fwd_tc_kern
                         tmem_wait_ld();
                         store_tile(2 * j, v0);
                         store_tile(2 * j + 1, v1);
+                    }
+                }
+                fence_async_smem();
+                tc_fence_before();
+                __syncthreads();
+            }
+        }
+        if (failed) break;
+    }
+    cp_async_wait_all();
+    // leaving early with a bulk copy still in flight: one more bounded wait for it, so
+    // that it does not land in shared memory after this CTA is gone
+    if (failed && staging) mbar_wait(sbar_a, sphase);
+    if (cur != nullptr && !failed) flush(cur);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(a.tmem_cols) : "memory");
+}
+
+// BF16 forward (layout and mode order in the file comment).  Same pipeline as
+// fwd_tc_kernel: one staging slot refilled by a bulk copy while the current entry's
+// modes run, factors one entry ahead in registers, runs of entries with one output
+// summed in TMEM, bounded mbarrier waits.
+__global__ void __launch_bounds__(kTcThreads, 8) fwd_tc_bf16_kernel(const TcArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int N = a.N, F = N / 8, d = a.d;
+    const int pairs = (a.tiles + 1) / 2;
+    float *raw = reinterpret_cast<float *>(smem_raw);                          // staging slot, N floats
+    unsigned char *xs = reinterpret_cast<unsigned char *>(raw + N);           // pairs x kPairBytes
+    unsigned char *bs = xs + (size_t)pairs * kPairBytes + 64;                 // d x [A_i 0; 0 A_i]
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(bs + (size_t)d * kBf16B);  // MMA completion
+    uint64_t *sbar = mbar + 1;                                                // staging completion
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 2);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    long long e = (long long)blockIdx.x * a.entries_per_cta;
+    const long long e_end = min(e + (long long)a.entries_per_cta, a.nb);
+    if (e >= e_end) return;
+
+    // operands zeroed once: fibres beyond F, the odd K half of an unpaired tile and the
+    // off-diagonal blocks of the factor operands stay zero
+    for (int v = tid; v < (int)(pairs * kPairBytes + 64 + d * kBf16B) / 16; v += kTcThreads)
+        reinterpret_cast<int4 *>(xs)[v] = make_int4(0, 0, 0, 0);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(a.tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    const uint32_t sbar_a = smem_u32(sbar);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sbar_a) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    TcPtrs nxt;
+    float fv[kTcFacSlots] = {0.f, 0.f};  // factor elements of the entry staged last
+    tc_load_ptrs(nxt, a, e, tid);
+    tc_stage_async(raw, fv, nxt, a, tid, sbar_a);
+    if (e + 1 < e_end) tc_load_ptrs(nxt, a, e + 1, tid);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t tacc = tmem + 16u * pairs;  // run accumulator after the mode output
+    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+    const uint32_t mbar_a = smem_u32(mbar);
+    const uint32_t xs_a = smem_u32(xs), bs_a = smem_u32(bs);
+    uint32_t phase = 0, sphase = 0;
+    bool failed = false;
+    bool staging = true;  // a staging copy is in flight whose phase has not been waited for
+    double *cur = nullptr;
+    constexpr int MAXP = 2;  // tile pairs per entry (N <= 4096)
+
+    // run sum (TMEM accumulator) -> FP64 reductions into `dst`.  Fibre c of the last mode
+    // holds output positions 8c + r; after an octet transpose lane l of octet o holds
+    // positions 64o + 8j + l (o = c / 8), so every reduction instruction of a warp covers
+    // 4 runs of 8 consecutive doubles.
+    auto flush = [&](double *dst) {
+        if (F < 8) {  // d = 1: one fibre, its 8 values are the whole output vector
+            if (warp == 0) {
+                float v0[8], v1[8];
+                tmem_ld16(tacc, v0, v1);  // warp-collective: the whole warp loads
+                tmem_wait_ld();
+                if (lane == 0)
+#pragma unroll
+                    for (int r = 0; r < 8; ++r) red_add_f64(dst + r, (double)v0[r]);
+            }
+            return;
+        }
+#pragma unroll
+        for (int j = 0; j < MAXP; ++j) {
+            if (j < pairs) {
+                float v0[8], v1[8];
+                tmem_ld16(tacc + lane_base + 16u * j, v0, v1);
+                tmem_wait_ld();
+                octet_transpose(v0, lane);
+                octet_transpose(v1, lane);
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int t = 2 * j + h;
+                    const int c0 = t * kTileRows + warp * 32 + (lane & ~7);  // first fibre of the octet
+                    if (t < a.tiles && c0 < F) {
+                        double *p = dst + 8 * c0 + (lane & 7);
+#pragma unroll
+                        for (int r = 0; r < 8; ++r) red_add_f64(p + 8 * r, (double)(h ? v1[r] : v0[r]));
+                    }
+                }
+            }
+        }
+    };
+
+    for (; e < e_end; ++e) {
+        double *o = a.out[e];
+        cp_async_wait_all();
+        const bool staged = mbar_wait(sbar_a, sphase);  // the slot's bulk copy (or its empty phase)
+        if (__syncthreads_or(!staged)) {  // slot complete for every thread; previous MMAs done
+            if (tid == 0) atomicCAS(&g_tc_error, 0u, 1u);
+            failed = true;
+            break;
+        }
+        sphase ^= 1u;
+        staging = false;
+        // factor operands: B_i[n][k] = A_i(n, k) in the upper-left and lower-right blocks
+#pragma unroll
+        for (int s = 0; s < kTcFacSlots; ++s) {
+            const int v = tid + s * kTcThreads;
+            if (v < d * 64) {
+                const int i = v >> 6, r = v & 7, k = (v >> 3) & 7;
+                put<KIND_BF16>(bs + (size_t)i * kBf16B, r, k, fv[s]);
+                put<KIND_BF16>(bs + (size_t)i * kBf16B, r + 8, k + 8, fv[s]);
+            }
+        }
+        // vector operand: natural position p = fibre + F*K (K = the slowest index, mode 0,
+        // contracted first), so 8 consecutive positions are 8 consecutive fibres of one K row
+        if (d == 1) {
+            if (tid < 8) *reinterpret_cast<__nv_bfloat16 *>(xs + tid * 16) = __float2bfloat16_rn(raw[tid]);
+        } else {
+            const uint32_t fsh = 3u * (uint32_t)(d - 1);
+            for (int q = tid; q < N / 8; q += kTcThreads) {
+                // the two 16-byte halves in an order that keeps each 8-lane phase of the
+                // 16-byte loads on 8 distinct bank slots
+                const int h = (q >> 2) & 1;
+                const float4 first = *reinterpret_cast<const float4 *>(raw + 8 * q + 4 * h);
+                const float4 second = *reinterpret_cast<const float4 *>(raw + 8 * q + 4 * (h ^ 1));
+                const float4 u = h ? second : first, w = h ? first : second;
+                const uint32_t p0 = 8u * (uint32_t)q;
+                *reinterpret_cast<uint4 *>(xs + mn_offset((p0 & (uint32_t)(F - 1)) >> 3, p0 >> fsh)) =
+                    pack_bf16x8(u.x, u.y, u.z, u.w, w.x, w.y, w.z, w.w);
+            }
+        }
+        // the run continues when this entry adds into the same output as the previous one;
+        // otherwise the previous run's sum leaves TMEM before the last mode overwrites it
+        const bool cont = (o == cur);
+        if (!cont && cur != nullptr) flush(cur);
+        cur = o;
+        fence_async_smem();  // the staging slot has been read (generic proxy) before the bulk copy refills it
+        tc_fence_before();
+        __syncthreads();
+        if (e + 1 < e_end) {
+            tc_stage_async(raw, fv, nxt, a, tid, sbar_a);
+            staging = true;
+            if (e + 2 < e_end) tc_load_ptrs(nxt, a, e + 2, tid);
+        }
+
+        for (int i = 0; i < d; ++i) {  // modes 0, 1, ..., d-1
+            const bool last = i == d - 1;
+            if (tid == 0) {
+                tc_fence_after();
+                const uint32_t dst = last ? tacc : tmem;
+                const uint32_t accumulate = (last && cont) ? 1u : 0u;
+                for (int j = 0; j < pairs; ++j)
+                    mma_bf16_mn(dst + 16u * (uint32_t)j, smem_desc(xs_a + j * kPairBytes, kMnLbo, kMnSbo),
+                                smem_desc(bs_a + i * kBf16B), accumulate);
+                mma_commit(mbar_a);
+            }
+            const bool ok = mbar_wait(mbar_a, phase);
+            // the decision to leave must be uniform: the TMEM loads below are warp-collective
+            if (__syncthreads_or(!ok)) {
+                if (tid == 0) atomicCAS(&g_tc_error, 0u, 1u);
+                failed = true;
+                break;
+            }
+            phase ^= 1u;
+            tc_fence_after();
+            if (!last) {
+                // fibre c = g + F/8 * kk with kk the next mode's index (c's top digit): the 8
+                // new values become the 8 consecutive fibres 8g..8g+7 of the next operand
+                const uint32_t sh = 3u * (uint32_t)(d - 2);
+#pragma unroll
+                for (int j = 0; j < MAXP; ++j) {
+                    if (j < pairs) {
+                        float v0[8], v1[8];
+                        tmem_ld16(tmem + lane_base + 16u * j, v0, v1);
+                        tmem_wait_ld();
+#pragma unroll
+                        for (int h = 0; h < 2; ++h) {
+                            const int t = 2 * j + h;
+                            const int c = t * kTileRows + warp * 32 + lane;
+                            if (t < a.tiles && c < F) {
+                                const float(&v)[8] = h ? v1 : v0;
+                                const uint32_t kk = (uint32_t)c >> sh, g = (uint32_t)c & ((1u << sh) - 1u);
+                                *reinterpret_cast<uint4 *>(xs + mn_offset(g, kk)) =
+                                    pack_bf16x8(v[0], v[1], v[2], v[3], v[4], v[5], v[6], v[7]);
+                            }
+                        }
                     }
                 }
                 fence_async_smem();
@@ -431,11 +731,15 @@ int launch_tc_forward(int kind, int d, int n, const float *const *mats, int stri
     a.N = (int)Nl;
     const int F = a.N / 8;
     a.tiles = (F + kTileRows - 1) / kTileRows;
+    const int pairs = (a.tiles + 1) / 2;
     int cols = 32;
-    while (cols < 2 * 16 * ((a.tiles + 1) / 2)) cols *= 2;  // mode output + run accumulator
+    while (cols < 2 * 16 * pairs) cols *= 2;  // mode output + run accumulator
     a.tmem_cols = cols;
-    const size_t need = (size_t)a.N * sizeof(float) + (size_t)a.tiles * kTileBytes + 64 +
-                        (size_t)2 * d * kBBytes + 32;  // + two mbarriers and the TMEM address
+    const bool bf16 = kind == KRONMULT_COMPUTE_BF16;
+    const size_t need = (size_t)a.N * sizeof(float) +
+                        (bf16 ? (size_t)pairs * kPairBytes + 64 + (size_t)d * kBf16B
+                              : (size_t)a.tiles * kTileBytes + 64 + (size_t)2 * d * kBBytes) +
+                        32;  // + two mbarriers and the TMEM address
     // resident CTAs per SM are limited so that their tensor-memory columns fit in 512
     // (or to tuning.ctas_per_sm when that is fewer): each CTA reserves 1/max_ctas of the
     // SM's shared memory (less the per-CTA system reservation), so at most max_ctas fit
@@ -445,8 +749,7 @@ int launch_tc_forward(int kind, int d, int n, const float *const *mats, int stri
     smem &= ~(size_t)15;
     if (smem < need) smem = need;
     if (smem > (size_t)di.max_smem_optin) return cudaErrorNotSupported;
-    const void *fn = kind == KRONMULT_COMPUTE_TF32 ? (const void *)fwd_tc_kernel<KIND_TF32>
-                                                   : (const void *)fwd_tc_kernel<KIND_BF16>;
+    const void *fn = bf16 ? (const void *)fwd_tc_bf16_kernel : (const void *)fwd_tc_kernel<KIND_TF32>;
     if (!ensure_smem_attr(fn, smem)) return cudaErrorInvalidValue;
     // runs of 8 consecutive entries per CTA (the fan-in of a typical output group) and as
     // many CTAs as that gives: the hardware keeps as many resident as the shared-memory
@@ -457,10 +760,10 @@ int launch_tc_forward(int kind, int d, int n, const float *const *mats, int stri
     a.entries_per_cta = (int)ept;
     const long long grid = (nb + ept - 1) / ept;
     if (grid > INT_MAX) return cudaErrorInvalidValue;
-    if (kind == KRONMULT_COMPUTE_TF32)
-        fwd_tc_kernel<KIND_TF32><<<(unsigned)grid, kTcThreads, smem, st>>>(a);
+    if (bf16)
+        fwd_tc_bf16_kernel<<<(unsigned)grid, kTcThreads, smem, st>>>(a);
     else
-        fwd_tc_kernel<KIND_BF16><<<(unsigned)grid, kTcThreads, smem, st>>>(a);
+        fwd_tc_kernel<KIND_TF32><<<(unsigned)grid, kTcThreads, smem, st>>>(a);
     return (int)cudaGetLastError();
 }
 
