@@ -49,8 +49,17 @@ struct Team {
     }
 };
 
-// output accumulation: red.global.add for float and double
-template <typename T> __device__ __forceinline__ void atomic_add(T *addr, T v) { atomicAdd(addr, v); }
+// output accumulation into global memory: red.global.add (an atomic addition that
+// returns nothing, so no result register waits for the round trip)
+template <typename T> __device__ __forceinline__ void atomic_add(T *addr, T v);
+template <> __device__ __forceinline__ void atomic_add<double>(double *addr, double v)
+{
+    asm volatile("red.global.add.f64 [%0], %1;" ::"l"(addr), "d"(v) : "memory");
+}
+template <> __device__ __forceinline__ void atomic_add<float>(float *addr, float v)
+{
+    asm volatile("red.global.add.f32 [%0], %1;" ::"l"(addr), "f"(v) : "memory");
+}
 
 // streaming 16-byte load (input vectors are read exactly once)
 __device__ __forceinline__ int4 ld_stream16(const void *p) { return __ldcs(reinterpret_cast<const int4 *>(p)); }

@@ -298,6 +298,46 @@ int plan_forward(FwdPlan<T, TO> &pl, int d, int n, const T *const *mats, int str
                 }
             }
         }
+        // FP32, n = 8, d = 3 or 4: two modes per shared-memory pass, a lane pair per
+        // 64-value bi-fibre (fwd_pair8_kernel), CTAs of 128 threads
+        if constexpr (sizeof(T) == 4) {
+            const bool want_pair8 = !single && n == 8 && (d == 3 || d == 4) && !(tune && tune->prefetch == 1) &&
+                                    !(tune && tune->team_size > 0);
+            if (want_pair8) {
+                const int tsp = N / 32;  // two lanes per bi-fibre: 128 (d = 4) or 16 (d = 3)
+                auto fn = fwd_pair_lookup<TO>(8, 1);
+                const int vpad = p8_elems(N);  // padded layout (p8_phys)
+                const int fpad = round_up(d * 64, 4);
+                const int team_elems = 2 * (vpad + fpad);
+                const int teams = 128 / tsp;
+                const size_t smem = (size_t)teams * team_elems * sizeof(T);
+                if (fn && smem <= (size_t)di.max_smem_optin && ensure_smem_attr((const void *)fn, smem)) {
+                    int per_sm = (tune && tune->ctas_per_sm > 0) ? tune->ctas_per_sm
+                                                                 : occupancy((const void *)fn, 128, smem);
+                    if (per_sm < 1) per_sm = 1;
+                    const long long total_teams = (long long)di.sms * per_sm * teams;
+                    long long ept = (tune && tune->entries_per_team > 0) ? tune->entries_per_team : 8;
+                    if (ept * total_teams > nb * 2) ept = (nb + total_teams - 1) / total_teams;
+                    if (ept < 1) ept = 1;
+                    const long long grid = (nb + ept * teams - 1) / (ept * teams);
+                    if (grid <= INT_MAX && ept <= INT_MAX) {
+                        a.team_size = tsp;
+                        a.teams_per_cta = teams;
+                        a.entries_per_team = (int)ept;
+                        a.team_elems = team_elems;
+                        a.vec_pad = vpad;
+                        a.fac_pad = fpad;
+                        a.prefetch = 1;
+                        pl.fn = (const void *)fn;
+                        pl.smem_path = true;
+                        pl.grid = dim3((unsigned)grid);
+                        pl.block = dim3(128);
+                        pl.smem = smem;
+                        return cudaSuccess;
+                    }
+                }
+            }
+        }
         // FP32, n = 2 or 4, d >= 2: two modes per shared-memory pass (fwd_pair_kernel)
         if constexpr (sizeof(T) == 4) {
             const bool want_pair = !single && (n == 2 || n == 4) && d >= 2 && !(tune && tune->prefetch == 1) &&

@@ -1,4 +1,4 @@
-// FP32 forward that applies two modes per shared-memory pass (n = 2 or 4).
+// FP32 forward that applies two modes per shared-memory pass (n = 2, 4 and 8).
 //
 // For FP32 the single-mode sweep is bound by shared-memory traffic (every mode
 // reads and writes the whole vector once) rather than by HBM or the FMA pipe.
@@ -16,26 +16,36 @@
 // stored with 16-byte chunk ch at physical chunk ch ^ ((ch >> 3) & 7): eight
 // consecutive bi-fibres then land in eight distinct bank groups, and the scalar
 // writes of 32 consecutive positions stay a permutation of one 128-byte row.
+//
+// n = 8 (team_forward_pairs8): a lane pair shares one 64-value bi-fibre X[a][b].
+// Lane h holds rows a = 4h..4h+3 and applies mode i to them (index b); the pair then
+// swaps halves with 16 shuffles so that lane h holds columns b = 4h..4h+3 of all 8
+// rows, and applies mode i-1 to them (index a).  Each factor column is read as two
+// 16-byte broadcast loads and feeds 32 FMAs; every output is still the k-ascending
+// FMA chain from 0 of the reference.
 #pragma once
 #include "fwd_kernels.cuh"
 
 namespace kgb {
 
 template <int NN> struct PairSwizzle {
-    // physical element index of logical element p (floats)
-    static __device__ __forceinline__ int elem(int p)
-    {
-        if constexpr (NN == 4) {
-            const int ch = p >> 2;
-            return ((ch ^ ((ch >> 3) & 7)) << 2) | (p & 3);
-        } else {
-            return p;
-        }
-    }
+    // physical 16-byte chunk of logical chunk ch (n = 4): the XOR of bits 3..5 keeps every
+    // aligned group of 8 chunks within itself (32 consecutive scalar positions stay one
+    // 128-byte row) and puts 8 consecutive 64-byte bi-fibres on 8 slots.  (n = 8 uses
+    // the padded layout of p8_phys instead.)
     static __device__ __forceinline__ int chunk(int ch)
     {
         if constexpr (NN == 4) return ch ^ ((ch >> 3) & 7);
         return ch;
+    }
+    // physical element index of logical element p (floats)
+    static __device__ __forceinline__ int elem(int p)
+    {
+        if constexpr (NN == 4) {
+            return (chunk(p >> 2) << 2) | (p & 3);
+        } else {
+            return p;
+        }
     }
 };
 
@@ -276,6 +286,293 @@ __device__ __forceinline__ void team_forward_pairs(const float *const *mats, con
     }
 }
 
+// ---- n = 8 --------------------------------------------------------------------
+
+// Shared-memory layout of the n = 8 pair path: bi-fibre q (64 values) at 72 q + 16 (q/4),
+// its two halves (rows 0..3 and 4..7, the halves of a lane pair) 36 floats apart.  The
+// 16-byte loads of a warp's 8-lane phase (4 bi-fibres x 2 halves) start on 8 distinct
+// bank slots; 32 consecutive positions stay within one 32-float half, and positions
+// 4 bi-fibres apart (the two halves of a warp's stores for d = 4) land 304 floats
+// apart, on the other 16 banks: the scalar stores are conflict-free.
+__device__ __forceinline__ int p8_phys(int p)
+{
+    return (p >> 6) * 72 + (p >> 8) * 16 + ((p >> 5) & 1) * 36 + (p & 31);
+}
+__host__ __device__ constexpr int p8_elems(int N) { return N / 64 * 72 + N / 256 * 16; }
+
+// factor elements a thread copies per entry through prefetched pointers (d*64 <= 4 x 64)
+constexpr int kPair8FacSlots = 4;
+struct Pair8Ptrs {
+    const float *src;
+    const float *mat[kPair8FacSlots];
+};
+
+__device__ __forceinline__ void pair8_load_ptrs(Pair8Ptrs &p, const float *const *in, const float *const *mats,
+                                                long long e, int d, const Team &tm)
+{
+    p.src = in[e];
+#pragma unroll
+    for (int s = 0; s < kPair8FacSlots; ++s) {
+        const int idx = tm.rank + s * tm.size;
+        p.mat[s] = idx < d * 64 ? mats[e * d + (idx >> 6)] : nullptr;
+    }
+}
+
+__device__ __forceinline__ void pair8_stage_async(float *dst, float *fac, const Pair8Ptrs &p,
+                                                  const float *const *mats_e, int N, int d, int stride,
+                                                  const Team &tm)
+{
+    if (((reinterpret_cast<uintptr_t>(p.src) & 15u) == 0) && ((N & 3) == 0)) {
+        for (int v = tm.rank; v < N / 4; v += tm.size) cp_async<16>(dst + p8_phys(4 * v), p.src + 4 * v);
+    } else {
+        for (int v = tm.rank; v < N; v += tm.size) cp_async<4>(dst + p8_phys(v), p.src + v);
+    }
+#pragma unroll
+    for (int s = 0; s < kPair8FacSlots; ++s) {
+        const int idx = tm.rank + s * tm.size;
+        if (idx < d * 64) {
+            const int k = (idx >> 3) & 7, r = idx & 7;
+            cp_async<4>(fac + idx, p.mat[s] + r + (size_t)k * stride);
+        }
+    }
+    // elements beyond the prefetched slots (small teams only): direct pointer loads
+    for (int idx = tm.rank + kPair8FacSlots * tm.size; idx < d * 64; idx += tm.size) {
+        const int i = idx >> 6, k = (idx >> 3) & 7, r = idx & 7;
+        cp_async<4>(fac + idx, mats_e[i] + r + (size_t)k * stride);
+    }
+    cp_async_commit();
+}
+
+// column k of a staged 8 x 8 factor (col-major, 16-byte aligned): two broadcast loads
+__device__ __forceinline__ void factor_col8(const float *M, int k, float (&col)[8])
+{
+    const float4 u = *reinterpret_cast<const float4 *>(M + 8 * k);
+    const float4 w = *reinterpret_cast<const float4 *>(M + 8 * k + 4);
+    col[0] = u.x; col[1] = u.y; col[2] = u.z; col[3] = u.w;
+    col[4] = w.x; col[5] = w.y; col[6] = w.z; col[7] = w.w;
+}
+
+// Team forward for n = 8 over entries [e_begin, e_end): a lane pair per bi-fibre
+// (team = 2*F2 threads), two staging slots; runs of equal output pointers summed in
+// registers (FP32) and added in the output type.  FMAs in packed FP32 pairs.
+template <typename TO>
+__device__ __forceinline__ void team_forward_pairs8(const float *const *mats, const float *const *in, TO *const *out,
+                                                    int d, int stride, int N, long long e_begin, long long e_end,
+                                                    float *buf, float *fac, float *buf2, float *fac2, const Team &tm)
+{
+    const int F = N / 8, F2 = N / 64;
+    const int c2 = tm.rank >> 1;  // this lane pair's bi-fibre
+    const int h = tm.rank & 1;    // rows 4h..4h+3, then columns 4h..4h+3
+    const unsigned pair_mask = tm.size >= 32 ? 0xffffffffu : tm.mask;
+    const f2 zero2 = f2_pack(0.f, 0.f);
+    // destination of element c2 + F2*(4h + rr + 8 ra): for d = 4 (F2 = 64, c2 < 64) it is
+    // p8_phys(c2) + 304 h + 72 rr + 608 ra (bi-fibre 4h + rr + 8 ra, group h + 2 ra)
+    const bool lin = F2 == 64;
+    const int dst0 = p8_phys(c2) + 304 * h;
+    f2 acc[4][4];  // acc[rr][j] = elements (rr, ra = 2j), (rr, 2j+1)
+    TO *cur = nullptr;
+
+    Pair8Ptrs nxt;
+    if (e_begin < e_end) {
+        pair8_load_ptrs(nxt, in, mats, e_begin, d, tm);
+        pair8_stage_async(buf, fac, nxt, mats + e_begin * d, N, d, stride, tm);
+        if (e_begin + 1 < e_end) pair8_load_ptrs(nxt, in, mats, e_begin + 1, d, tm);
+    }
+    for (long long e = e_begin; e < e_end; ++e) {
+        TO *o = out[e];
+        cp_async_wait_all();
+        tm.sync();
+        if (e + 1 < e_end) {
+            pair8_stage_async(buf2, fac2, nxt, mats + (e + 1) * d, N, d, stride, tm);
+            if (e + 2 < e_end) pair8_load_ptrs(nxt, in, mats, e + 2, d, tm);
+        }
+
+        int i = d - 1;
+        if (d & 1) {
+            // one single-mode step (mode d-1) over the F fibres, at most 4 per thread
+            const float *M = fac + i * 64;
+            f2 y[4][4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int c = tm.rank + q * tm.size;
+                if (c < F) {
+                    const float *src = buf + p8_phys(8 * c);
+                    const float4 u = *reinterpret_cast<const float4 *>(src);
+                    const float4 w = *reinterpret_cast<const float4 *>(src + 4);
+                    const float xv[8] = {u.x, u.y, u.z, u.w, w.x, w.y, w.z, w.w};
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        const float4 m0 = *reinterpret_cast<const float4 *>(M + 8 * k);
+                        const float4 m1 = *reinterpret_cast<const float4 *>(M + 8 * k + 4);
+                        const f2 col[4] = {f2_pack(m0.x, m0.y), f2_pack(m0.z, m0.w), f2_pack(m1.x, m1.y),
+                                           f2_pack(m1.z, m1.w)};
+                        const f2 xk = f2_pack(xv[k], xv[k]);
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) y[q][j] = f2_fma(col[j], xk, k == 0 ? zero2 : y[q][j]);
+                    }
+                }
+            }
+            tm.sync();
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int c = tm.rank + q * tm.size;
+                if (c < F) {
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        float lo, hi;
+                        f2_unpack(y[q][j], lo, hi);
+                        buf[p8_phys(c + 2 * j * F)] = lo;
+                        buf[p8_phys(c + (2 * j + 1) * F)] = hi;
+                    }
+                }
+            }
+            tm.sync();
+            --i;
+        }
+        f2 z[4][4];  // z[rr][j]: elements c2 + F2*(4h + rr + 8 ra), ra = 2j, 2j+1
+        for (; i >= 1; i -= 2) {
+            const float *M1 = fac + i * 64;        // acts on index b (fastest)
+            const float *M0 = fac + (i - 1) * 64;  // then on index a
+            float x[4][8];                         // rows 4h + aa
+            {
+                const float *src = buf + p8_phys(64 * c2) + 36 * h;
+#pragma unroll
+                for (int aa = 0; aa < 4; ++aa) {
+                    const float4 u = *reinterpret_cast<const float4 *>(src + 8 * aa);
+                    const float4 w = *reinterpret_cast<const float4 *>(src + 8 * aa + 4);
+                    x[aa][0] = u.x; x[aa][1] = u.y; x[aa][2] = u.z; x[aa][3] = u.w;
+                    x[aa][4] = w.x; x[aa][5] = w.y; x[aa][6] = w.z; x[aa][7] = w.w;
+                }
+            }
+            // mode i on b, for this lane's 4 rows
+            {
+                f2 t[4][4];
+#pragma unroll
+                for (int b = 0; b < 8; ++b) {
+                    const float4 m0 = *reinterpret_cast<const float4 *>(M1 + 8 * b);
+                    const float4 m1 = *reinterpret_cast<const float4 *>(M1 + 8 * b + 4);
+                    const f2 col[4] = {f2_pack(m0.x, m0.y), f2_pack(m0.z, m0.w), f2_pack(m1.x, m1.y),
+                                       f2_pack(m1.z, m1.w)};
+#pragma unroll
+                    for (int aa = 0; aa < 4; ++aa) {
+                        const f2 xb = f2_pack(x[aa][b], x[aa][b]);
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) t[aa][j] = f2_fma(col[j], xb, b == 0 ? zero2 : t[aa][j]);
+                    }
+                }
+#pragma unroll
+                for (int aa = 0; aa < 4; ++aa)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) f2_unpack(t[aa][j], x[aa][2 * j], x[aa][2 * j + 1]);
+            }
+            // swap halves with the partner lane: keep columns 4h..4h+3 of the own rows,
+            // send columns 4(1-h).. and receive the partner's rows at columns 4h..
+            float lo[4][4], hi[4][4];  // rows 0..3 and 4..7 of this lane's 4 columns
+#pragma unroll
+            for (int aa = 0; aa < 4; ++aa) {
+#pragma unroll
+                for (int rr = 0; rr < 4; ++rr) {
+                    const float own = h ? x[aa][4 + rr] : x[aa][rr];
+                    const float send = h ? x[aa][rr] : x[aa][4 + rr];
+                    const float recv = __shfl_xor_sync(pair_mask, send, 1);
+                    lo[aa][rr] = h ? recv : own;
+                    hi[aa][rr] = h ? own : recv;
+                }
+            }
+            // mode i-1 on a, for this lane's 4 columns, a ascending
+#pragma unroll
+            for (int a = 0; a < 8; ++a) {
+                const float4 m0 = *reinterpret_cast<const float4 *>(M0 + 8 * a);
+                const float4 m1 = *reinterpret_cast<const float4 *>(M0 + 8 * a + 4);
+                const f2 col[4] = {f2_pack(m0.x, m0.y), f2_pack(m0.z, m0.w), f2_pack(m1.x, m1.y),
+                                   f2_pack(m1.z, m1.w)};
+#pragma unroll
+                for (int rr = 0; rr < 4; ++rr) {
+                    const float xa = a < 4 ? lo[a & 3][rr] : hi[a & 3][rr];
+                    const f2 x2 = f2_pack(xa, xa);
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) z[rr][j] = f2_fma(col[j], x2, a == 0 ? zero2 : z[rr][j]);
+                }
+            }
+            tm.sync();  // every read of buf (and fac) for this pass is done
+            if (i > 1) {
+#pragma unroll
+                for (int rr = 0; rr < 4; ++rr) {
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        float v0, v1;
+                        f2_unpack(z[rr][j], v0, v1);
+                        const int r0 = rr + 8 * (2 * j), r1 = rr + 8 * (2 * j + 1);
+                        if (lin) {
+                            buf[dst0 + 72 * rr + 608 * (2 * j)] = v0;
+                            buf[dst0 + 72 * rr + 608 * (2 * j + 1)] = v1;
+                        } else {
+                            buf[p8_phys(c2 + F2 * (4 * h + r0))] = v0;
+                            buf[p8_phys(c2 + F2 * (4 * h + r1))] = v1;
+                        }
+                    }
+                }
+                tm.sync();
+            }
+        }
+        if (o != cur) {
+            if (cur != nullptr) {
+#pragma unroll
+                for (int rr = 0; rr < 4; ++rr)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        float v0, v1;
+                        f2_unpack(acc[rr][j], v0, v1);
+                        atomic_add<TO>(cur + c2 + F2 * (4 * h + rr + 8 * (2 * j)), (TO)v0);
+                        atomic_add<TO>(cur + c2 + F2 * (4 * h + rr + 8 * (2 * j + 1)), (TO)v1);
+                    }
+            }
+            cur = o;
+#pragma unroll
+            for (int rr = 0; rr < 4; ++rr)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[rr][j] = z[rr][j];
+        } else {
+#pragma unroll
+            for (int rr = 0; rr < 4; ++rr)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[rr][j] = f2_add(acc[rr][j], z[rr][j]);
+        }
+        float *t = buf;
+        buf = buf2;
+        buf2 = t;
+        t = fac;
+        fac = fac2;
+        fac2 = t;
+    }
+    if (cur != nullptr) {
+#pragma unroll
+        for (int rr = 0; rr < 4; ++rr)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                float v0, v1;
+                f2_unpack(acc[rr][j], v0, v1);
+                atomic_add<TO>(cur + c2 + F2 * (4 * h + rr + 8 * (2 * j)), (TO)v0);
+                atomic_add<TO>(cur + c2 + F2 * (4 * h + rr + 8 * (2 * j + 1)), (TO)v1);
+            }
+    }
+}
+
+// One CTA of 128 threads: teams of 2*F2 threads (128 for d = 4, 16 for d = 3).
+template <typename TO> __global__ void __launch_bounds__(128, 3) fwd_pair8_kernel(const FwdArgs<float, TO> a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const Team tm(a.team_size);
+    float *buf = reinterpret_cast<float *>(smem_raw) + (size_t)tm.id * a.team_elems;
+    float *fac = buf + a.vec_pad;
+    float *buf2 = fac + a.fac_pad;
+    float *fac2 = buf2 + a.vec_pad;
+    const long long team_global = (long long)blockIdx.x * a.teams_per_cta + tm.id;
+    const long long e = team_global * a.entries_per_team;
+    const long long e_end = min(e + (long long)a.entries_per_team, a.nb);
+    team_forward_pairs8<TO>(a.mats, a.in, a.out, a.d, a.stride, a.N, e, e_end, buf, fac, buf2, fac2, tm);
+}
+
 template <typename TO, int NN, int QP>
 __global__ void __launch_bounds__(256, 3) fwd_pair_kernel(const FwdArgs<float, TO> a)
 {
@@ -304,6 +601,7 @@ template <typename TO> FwdSmemFn<float, TO> fwd_pair_lookup(int nn, int qp);
         case 2 * 16 + 2: return fwd_pair_kernel<TO, 2, 2>;                                             \
         case 4 * 16 + 1: return fwd_pair_kernel<TO, 4, 1>;                                             \
         case 4 * 16 + 2: return fwd_pair_kernel<TO, 4, 2>;                                             \
+        case 8 * 16 + 1: return fwd_pair8_kernel<TO>;                                                  \
         default: return nullptr;                                                                       \
         }                                                                                              \
     }                                                                                                  \

@@ -260,10 +260,10 @@ def test_cpp_drop_in_runs(cuda, tmp_path):
     assert p.returncode == 0, p.stdout + p.stderr
 
 
-@pytest.mark.parametrize("n,d", [(2, 2), (2, 3), (2, 9), (4, 2), (4, 3), (4, 5), (4, 6)])
+@pytest.mark.parametrize("n,d", [(2, 2), (2, 3), (2, 9), (4, 2), (4, 3), (4, 5), (4, 6), (8, 3), (8, 4)])
 def test_fp32_two_modes_per_pass(cuda, n, d):
-    """FP32 n = 2, 4 runs two modes per shared-memory pass (odd d: one single step
-    first); same result as the oracle's FP32 sweep up to FP32 rounding."""
+    """FP32 n = 2, 4 and 8 (d = 3, 4) runs two modes per shared-memory pass (odd d: one
+    single step first); same result as the oracle's FP32 sweep up to FP32 rounding."""
     from kronmult_gb300 import workloads as W
 
     b = W.make_batch(d, n, n + 3, 6, 7, seed=400 + 10 * n + d)

@@ -64,12 +64,15 @@ def test_bitwise_per_entry_large(cuda, d, n, stride, dtype):
     assert torch.equal(db.outputs, want)
 
 
-def test_bitwise_per_entry_f32(cuda):
+@pytest.mark.parametrize("d,n,stride", [(6, 4, 8), (4, 8, 8), (3, 8, 11)])
+def test_bitwise_per_entry_f32(cuda, d, n, stride):
+    """FP32 two-modes-per-pass kernels (n = 4; n = 8 with a lane pair per bi-fibre)
+    against the reference float kernel: identical bits per entry."""
     needs_ref()
     from kronmult_gb300 import DeviceBatch
     from kronmult_gb300 import workloads as W
 
-    b = W.make_batch(6, 4, 8, 40, 1, seed=650, block=64)
+    b = W.make_batch(d, n, stride, 40, 1, seed=650 + d, block=n * stride)
     db = DeviceBatch.from_host(b, device=cuda, dtype=torch.float32)
     want = reference_run(db, "f32")
     db.forward(sync=True)
