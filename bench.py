@@ -582,6 +582,27 @@ def suite(args):
             # x and g read, grad_input written, factors read and grad_A written, outputs once
             return b.bytes(i, o) + i * b.N * b.nb * 2 + 2.0 * i * b.n * b.n * b.d * b.n_sets
 
+    # the grouped form: one plan holding the forward group and the adjoint group, FP32,
+    # replayed from one CUDA graph (forward and adjoint run as parallel branches)
+    db = DeviceBatch.from_host(b, device=dev, dtype=torch.float32)
+    gt = torch.from_numpy(gout).to(dev, torch.float32)
+    gin = torch.zeros_like(db.inputs)
+    gfa = torch.zeros_like(db.factors)
+    plan = G.GroupedPlan([db], mode="atomic", adjoints=[(db, gt, gin, gfa)])
+    with torch.cuda.stream(st):
+        plan.run(stream=st)
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=st):
+        plan.run(stream=st)
+    m32g = _timed(lambda: graph.replay(), torch.cuda.current_stream(), reps)
+    for t in (db.outputs, gin, gfa):
+        t.zero_()
+    graph.replay()
+    torch.cuda.synchronize()
+    y32g, gi32g, ga32g = (t.double().cpu().numpy() for t in (db.outputs, gin, gfa))
+    plan.close()
+
     fm = {"flops_model": "3 x 2dnN per entry (forward, grad_input, grad_A contractions; "
                          "the partial products grad_A needs are not counted)"}
     emit("c5_fwd_adj_f64_plain", _FwdAdj(), m64, 8, 8, fm, launches=2)
@@ -589,6 +610,11 @@ def suite(args):
         "speedup_vs_plain_fp64": m64 / m32,
         "rel_l2_vs_fp64": {"output": O.rel_l2(y32, y64), "grad_input": O.rel_l2(gi32, gi64),
                            "grad_factors": O.rel_l2(ga32, ga64)}}, launches=2)
+    emit("c5_fwd_adj_f32_grouped_graph", _FwdAdj(), m32g, 4, 4, {**fm,
+        "speedup_vs_plain_fp64": m64 / m32g,
+        "form": "one grouped plan (forward group + adjoint group as parallel branches), one graph replay",
+        "rel_l2_vs_fp64": {"output": O.rel_l2(y32g, y64), "grad_input": O.rel_l2(gi32g, gi64),
+                           "grad_factors": O.rel_l2(ga32g, ga64)}}, launches=2)
 
 
 def main():

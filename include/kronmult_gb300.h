@@ -130,14 +130,30 @@ int kronmult_batched_adjoint_f32_async(int matrix_count, int matrix_size, const 
  * Grouped persistent forward (no reference counterpart; the reference serves one
  * (d, n) per call, kronmult_gpu/kronmult.cu:173-197).  Each group is one
  * kronmult_batched call's worth of arguments (device pointer tables).  A plan is
- * built once -- it reads the output pointer tables, orders the entries of each
- * group by output pointer for the deterministic mode, cuts the work into items
- * and uploads them -- and kronmult_grouped_run then enqueues one persistent
- * kernel that pulls the items from a device queue.  The run only enqueues a
- * memset and a kernel, so it can be captured in a CUDA graph.  Rebuild the plan
- * if the pointer tables change.  In the deterministic mode no output vector may
- * be shared between groups (cudaErrorInvalidValue).  Supports 2 <= n <= 16 with
- * n^d <= 2048 (FP64) or 4096 (FP32) (cudaErrorNotSupported otherwise).
+ * built once; kronmult_grouped_run then enqueues, per group, one persistent kernel
+ * compiled for that group's n (2..8; n = 9..16 take n at run time) whose teams pull
+ * work units from the group's device queue.  In the atomic mode the groups' kernels
+ * run as parallel branches (forked from `stream` and joined back into it through
+ * events); in the deterministic mode they run one after another on `stream`.  The
+ * run enqueues only a memset, kernels and event waits, so it can be captured in a
+ * CUDA graph.
+ *
+ * Deterministic mode: at plan creation every group's entries are ordered by output
+ * pointer ON THE DEVICE (a sort of (pointer, entry index) pairs: equal pointers keep
+ * their entry order) -- no device-to-host copy; plan creation waits for it.  Every
+ * output vector is then owned by one team, which sums its entries in entry order and
+ * adds the sum with one plain read-modify-write, out + ((y_0 + y_1) + ...), so the
+ * result is bitwise reproducible.  If a group's pointer tables change in place,
+ * kronmult_grouped_regroup re-runs that ordering on a stream (capturable too) before
+ * the next run.  Outputs may be shared between groups (the groups run in order).
+ *
+ * Atomic mode: runs of consecutive entries with one output pointer are summed in
+ * registers and added with atomics, as kronmult_batched does; the plan reads none of
+ * the tables.
+ *
+ * Supports 2 <= n <= 16 with n^d small enough for one team's shared memory
+ * (cudaErrorNotSupported otherwise).  tunings[g].team_size forces a team size,
+ * tunings[g].entries_per_team the work unit (entries per queue item).
  */
 typedef struct kronmult_group {
     int matrix_count, matrix_size, matrix_stride, nb_batch;
@@ -151,9 +167,38 @@ typedef struct kronmult_grouped_plan_s *kronmult_grouped_plan;
 int kronmult_grouped_plan_create(kronmult_grouped_plan *plan, const kronmult_group *groups, int n_groups, int dtype,
                                  int mode, const kronmult_tuning *tunings);
 int kronmult_grouped_run(kronmult_grouped_plan plan, void *stream);
-/* info[0..5] = grid, block, dynamic shared bytes, queue items, team ranges, permuted entries */
+/* info[0..5] = largest grid, block, largest dynamic shared bytes, work units (all
+ * groups), kernels per run (forward groups + adjoint groups), entries ordered on the
+ * device (deterministic mode) */
 int kronmult_grouped_plan_info(kronmult_grouped_plan plan, long long *info, int n_info);
 int kronmult_grouped_plan_destroy(kronmult_grouped_plan plan);
+/* Re-runs the deterministic mode's device-side ordering of every group on `stream`
+ * (after a pointer table changed in place: the deterministic run reads copies of the
+ * tables in sorted order, made by this ordering); a no-op in the atomic mode. */
+int kronmult_grouped_regroup(kronmult_grouped_plan plan, void *stream);
+
+/*
+ * Adjoint groups in a grouped plan (no reference counterpart): one
+ * kronmult_batched_adjoint call's worth of arguments each.  A plan made with
+ * kronmult_grouped_plan_create_with_adjoint runs, besides its forward groups, every
+ * adjoint group with the adjoint kernel as one more parallel branch of the same run
+ * (adjoint gradients are always added with atomics), so that one captured graph
+ * replays a whole forward + backward step.  The adjoint does not read the forward's
+ * outputs: the branches are independent.
+ */
+typedef struct kronmult_adjoint_group {
+    int matrix_count, matrix_size, matrix_stride, nb_batch;
+    const void *const *matrix_list_batched;  /* nb*d device pointers */
+    const void *const *input_batched;        /* nb device pointers */
+    const void *const *grad_output_batched;  /* nb device pointers (gradient of each entry's output) */
+    void *const *grad_input_batched;         /* nb device pointers, or NULL */
+    void *const *grad_matrix_list_batched;   /* nb*d device pointers, or NULL */
+    int grad_matrix_stride;
+} kronmult_adjoint_group;
+
+int kronmult_grouped_plan_create_with_adjoint(kronmult_grouped_plan *plan, const kronmult_group *groups,
+                                              int n_groups, const kronmult_adjoint_group *adjoint_groups,
+                                              int n_adjoint, int dtype, int mode, const kronmult_tuning *tunings);
 
 /*
  * Autotuner (no reference counterpart): times every valid launch shape of the

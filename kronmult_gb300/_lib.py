@@ -31,6 +31,16 @@ class Group(ctypes.Structure):
                 ("input_batched", ctypes.c_void_p), ("output_batched", ctypes.c_void_p)]
 
 
+class AdjointGroup(ctypes.Structure):
+    """Mirror of `kronmult_adjoint_group`: one adjoint group's arguments."""
+
+    _fields_ = [("matrix_count", ctypes.c_int), ("matrix_size", ctypes.c_int), ("matrix_stride", ctypes.c_int),
+                ("nb_batch", ctypes.c_int), ("matrix_list_batched", ctypes.c_void_p),
+                ("input_batched", ctypes.c_void_p), ("grad_output_batched", ctypes.c_void_p),
+                ("grad_input_batched", ctypes.c_void_p), ("grad_matrix_list_batched", ctypes.c_void_p),
+                ("grad_matrix_stride", ctypes.c_int)]
+
+
 KRONMULT_DTYPE_F64 = 0
 KRONMULT_DTYPE_F32 = 1
 KRONMULT_DTYPE_F32_F64OUT = 2
@@ -65,7 +75,10 @@ SIGNATURES = {
     "kronmult_batched_adjoint_f32_async": (_i, [_i, _i, _vp, _i, _vp, _vp, _vp, _vp, _i, _i, _vp, _TP]),
     "kronmult_grouped_plan_create": (_i, [ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(Group), _i, _i, _i,
                                          _TP]),
+    "kronmult_grouped_plan_create_with_adjoint": (_i, [ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(Group), _i,
+                                                      ctypes.POINTER(AdjointGroup), _i, _i, _i, _TP]),
     "kronmult_grouped_run": (_i, [_vp, _vp]),
+    "kronmult_grouped_regroup": (_i, [_vp, _vp]),
     "kronmult_grouped_plan_info": (_i, [_vp, ctypes.POINTER(ctypes.c_longlong), _i]),
     "kronmult_grouped_plan_destroy": (_i, [_vp]),
     "kronmult_autotune_forward": (_i, [_i, _i, _i, _i, _TP, ctypes.POINTER(ctypes.c_float)]),

@@ -1,23 +1,22 @@
-// Grouped, persistent forward: one launch serves several groups of entries with
-// different (d, n, fan-in), pulling work items from a device queue.
+// Grouped forward (and adjoint) plans: several groups of entries with different
+// (d, n, fan-in) served by one run that can be captured in a CUDA graph.
 //
-// No reference counterpart: the reference serves one (d, n) per call with one
-// CTA per entry (kronmult_gpu/kronmult.cu:173-197).  Two output modes:
-//  - atomic: runs of equal output pointers are summed in registers and added
-//    with atomics (same semantics as kronmult_batched);
-//  - deterministic: at plan time the entries of every group are ordered by output
-//    pointer (a stable sort; the identity when equal pointers are already
-//    contiguous) and cut into segments of equal pointer; each segment is summed
-//    by one team in entry order and added with one plain read-modify-write, so
-//    the result is bitwise reproducible from run to run.
-// The plan holds everything in device memory, so kronmult_grouped_run is a
-// memset of the two queue counters plus one kernel launch: it can be captured
-// in a CUDA graph and replayed.
+// No reference counterpart: the reference serves one (d, n) per call with one CTA
+// per entry (kronmult_gpu/kronmult.cu:173-197).  The plan gives every forward group a
+// persistent kernel compiled for its n (grouped_kernels.cuh) with a device work
+// queue; the run forks the groups' kernels (and any adjoint groups) into parallel
+// branches and joins them back into the caller's stream.  Two output modes:
+//  - atomic: runs of equal output pointers are summed in registers and added with
+//    atomics (same semantics as kronmult_batched);
+//  - deterministic: each group's entries are ordered by output pointer on the device
+//    (a bitonic sort of (pointer, entry index) pairs, which equals a stable sort by
+//    pointer) and every output vector is owned by one team, which sums its entries
+//    in entry order (in shared memory) and adds the sum with one plain
+//    read-modify-write: bitwise reproducible.
+//    The forward groups then run one after another, so an output may also be
+//    shared by groups.
 #include <algorithm>
 #include <climits>
-#include <cstring>
-#include <map>
-#include <numeric>
 #include <vector>
 #include "fwd_launch.cuh"
 #include "grouped.cuh"
@@ -25,109 +24,239 @@
 
 namespace kgb {
 
-// Every group runs the element-mapped team forward (runtime n): all lanes busy for
-// any (d, n), and one small register footprint for the whole persistent kernel.
-template <typename T, typename TO, bool DET>
-__device__ __forceinline__ void grouped_dispatch(const GroupDesc &g, long long b, long long e, T *slots,
-                                                 const Team &tm)
+// ---- device-side ordering by output pointer --------------------------------
+namespace {
+
+constexpr int kSortLocal = 2048;  // elements one CTA sorts in shared memory (1024 threads, 2 each)
+
+__global__ void gq_sort_init(const void *const *out, long long nb, long long m, unsigned long long *keys,
+                             long long *perm)
 {
-    const T *const *mats = reinterpret_cast<const T *const *>(g.mats);
-    const T *const *in = reinterpret_cast<const T *const *>(g.in);
-    TO *const *out = reinterpret_cast<TO *const *>(g.out);
-    const T **ptrs = reinterpret_cast<const T **>(slots + 2 * (size_t)g.vec_pad);
-#define KGB_G(EM)                                                                                      \
-    case EM:                                                                                           \
-        team_forward_elem_pf<T, TO, EM, DET>(mats, in, out, g.perm, g.d, g.n, g.stride, g.N, b, e, slots,       \
-                                             g.vec_pad, ptrs, tm);                                      \
-        break;
-    switch (g.emax) {
-        KGB_G(1) KGB_G(2) KGB_G(4)
-    case 8:
-        // FP64 teams hold at most 4 outputs per thread (80 registers, 3 CTAs per SM)
-        if constexpr (sizeof(T) == 4)
-            team_forward_elem_pf<T, TO, 8, DET>(mats, in, out, g.perm, g.d, g.n, g.stride, g.N, b, e, slots,
-                                                g.vec_pad, ptrs, tm);
-        break;
-    case 16:
-        if constexpr (sizeof(T) == 4)
-            team_forward_elem_pf<T, TO, 16, DET>(mats, in, out, g.perm, g.d, g.n, g.stride, g.N, b, e, slots,
-                                                 g.vec_pad, ptrs, tm);
-        break;
-    default: break;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m; i += (long long)gridDim.x * blockDim.x) {
+        keys[i] = i < nb ? (unsigned long long)reinterpret_cast<uintptr_t>(out[i]) : ~0ull;
+        perm[i] = i;
     }
-#undef KGB_G
 }
 
-template <typename T, typename TO, bool DET>
-__global__ void __launch_bounds__(kGroupedBlock, sizeof(T) == 8 ? 3 : 2)
-    grouped_kernel(const GroupDesc *groups, const CtaItem *items, int n_items, const TeamRange *ranges,
-                   unsigned *counters)
+// (key, index) pairs in lexicographic order: equal keys keep their entry order
+__device__ __forceinline__ bool pair_gt(unsigned long long ka, long long pa, unsigned long long kb, long long pb)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ int s_item;
-    for (;;) {
-        if (threadIdx.x == 0) s_item = (int)atomicAdd(&counters[0], 1u);
-        __syncthreads();
-        const int it = s_item;
-        __syncthreads();
-        if (it >= n_items) break;
-        const CtaItem ci = items[it];
-        const GroupDesc g = groups[ci.group];
-        const int team_id = threadIdx.x / g.team_size;
-        if (team_id < ci.count) {
-            const Team tm(g.team_size);
-            T *slots = reinterpret_cast<T *>(smem_raw) + (size_t)team_id * g.team_elems;
-            const TeamRange r = ranges[ci.first_range + team_id];
-            grouped_dispatch<T, TO, DET>(g, r.begin, r.end, slots, tm);
+    return ka > kb || (ka == kb && pa > pb);
+}
+
+// one compare-exchange step of the bitonic network (partner distance j >= kSortLocal)
+__global__ void gq_sort_step(unsigned long long *keys, long long *perm, long long m, long long j, long long k)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m; i += (long long)gridDim.x * blockDim.x) {
+        const long long l = i ^ j;
+        if (l <= i) continue;
+        const unsigned long long ki = keys[i], kl = keys[l];
+        const long long pi = perm[i], pl = perm[l];
+        const bool up = (i & k) == 0;
+        if (pair_gt(ki, pi, kl, pl) == up) {
+            keys[i] = kl;
+            keys[l] = ki;
+            perm[i] = pl;
+            perm[l] = pi;
         }
-        __syncthreads();
     }
 }
 
-// ---------------------------------------------------------------------------
-
-const void *grouped_kernel_ptr(int dtype, int mode)
+// every step with partner distance j <= jmax (< kSortLocal) of the stages k in
+// [k_first, k_last], inside one 2048-element chunk in shared memory
+__global__ void __launch_bounds__(1024) gq_sort_local(unsigned long long *keys, long long *perm, long long k_first,
+                                                      long long k_last, long long jmax)
 {
-    if (dtype == KRONMULT_DTYPE_F64)
-        return mode == KRONMULT_MODE_DETERMINISTIC ? (const void *)grouped_kernel<double, double, true>
-                                                   : (const void *)grouped_kernel<double, double, false>;
-    return mode == KRONMULT_MODE_DETERMINISTIC ? (const void *)grouped_kernel<float, float, true>
-                                               : (const void *)grouped_kernel<float, float, false>;
+    __shared__ unsigned long long sk[kSortLocal];
+    __shared__ long long sp[kSortLocal];
+    const long long base = (long long)blockIdx.x * kSortLocal;
+    for (int t = threadIdx.x; t < kSortLocal; t += blockDim.x) {
+        sk[t] = keys[base + t];
+        sp[t] = perm[base + t];
+    }
+    __syncthreads();
+    for (long long k = k_first; k <= k_last; k <<= 1) {
+        for (long long j = (k >> 1) < jmax ? (k >> 1) : jmax; j > 0; j >>= 1) {
+            const int t = threadIdx.x;  // pair t: positions i and i + j
+            const int i = (int)((t / j) * 2 * j + (t % j));
+            const int l = i + (int)j;
+            const bool up = ((base + i) & k) == 0;
+            const unsigned long long ki = sk[i], kl = sk[l];
+            const long long pi = sp[i], pl = sp[l];
+            if (pair_gt(ki, pi, kl, pl) == up) {
+                sk[i] = kl;
+                sk[l] = ki;
+                sp[i] = pl;
+                sp[l] = pi;
+            }
+            __syncthreads();
+        }
+    }
+    for (int t = threadIdx.x; t < kSortLocal; t += blockDim.x) {
+        keys[base + t] = sk[t];
+        perm[base + t] = sp[t];
+    }
 }
 
-// Element mapping: the team whose lanes are best used over the N outputs of an
-// entry; among equally good teams the one closest to 8 outputs per thread (enough
-// independent FMA chains per thread, few threads per barrier).  FP64 teams hold at
-// most 4 outputs per thread: the persistent kernel carries the register footprint
-// of its largest variant, and 4 keeps it at 80 registers (3 CTAs per SM, measured
-// 6 % faster on the four uneven groups than 8 per thread at 2 CTAs per SM).
-static int team_shape(int d, int n, int elem, const kronmult_tuning *tune, int &ts, int &qmax, int &team_elems,
-                      int &vec_pad, int &emax)
+// the group's pointer tables in sorted order
+__global__ void gq_gather(const void *const *mats, const void *const *in, const void *const *out, int d, long long nb,
+                          const long long *perm, const void **s_mats, const void **s_in, void **s_out)
+{
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nb; k += (long long)gridDim.x * blockDim.x) {
+        const long long p = perm[k];
+        s_in[k] = in[p];
+        s_out[k] = const_cast<void *>(out[p]);
+        for (int i = 0; i < d; ++i) s_mats[k * d + i] = mats[p * d + i];
+    }
+}
+
+}  // namespace
+
+void gq_group_launch(const void *const *mats, const void *const *in, const void *const *out, int d, long long nb,
+                     long long m, unsigned long long *keys, long long *perm, const void **s_mats,
+                     const void **s_in, void **s_out, cudaStream_t st)
+{
+    const unsigned grid = (unsigned)std::min<long long>((m + 255) / 256, 4096);
+    gq_sort_init<<<grid, 256, 0, st>>>(out, nb, m, keys, perm);
+    const unsigned chunks = (unsigned)(m / kSortLocal);
+    // stages up to kSortLocal entirely inside the chunks
+    gq_sort_local<<<chunks, 1024, 0, st>>>(keys, perm, 2, kSortLocal, kSortLocal / 2);
+    for (long long k = 2 * kSortLocal; k <= m; k <<= 1) {
+        for (long long j = k >> 1; j >= kSortLocal; j >>= 1) gq_sort_step<<<grid, 256, 0, st>>>(keys, perm, m, j, k);
+        gq_sort_local<<<chunks, 1024, 0, st>>>(keys, perm, k, k, kSortLocal / 2);
+    }
+    const unsigned ggrid = (unsigned)std::min<long long>((nb + 255) / 256, 4096);
+    gq_gather<<<ggrid, 256, 0, st>>>(mats, in, out, d, nb, perm, s_mats, s_in, s_out);
+}
+
+// ---- planning ----------------------------------------------------------------
+
+namespace {
+
+struct GqShape {
+    GqFn fn = nullptr;
+    int ts = 0, team_elems = 0, vec_pad = 0;
+};
+
+// The single-call planner's choice, for one team per entry at a time: fibre mapping
+// with a compile-time n (team size from the same target of fibres per thread), or
+// for FP64 the element mapping when it uses the lanes clearly better (by > 5
+// points); n = 9..16 take the element mapping with n at run time.
+template <typename T, typename TO>
+int gq_shape(int d, int n, bool det, const kronmult_tuning *tune, GqShape &sh)
 {
     const long long Nl = pow_ll(n, d);
     if (n < 2 || n > 16 || d < 1 || Nl > (long long)INT_MAX) return cudaErrorNotSupported;
-    const int N = (int)Nl;
-    ts = elem_team_size(N, elem == 8 ? 4 : 16, tune && tune->team_size > 0 ? tune->team_size : 0, kGroupedBlock);
-    if (ts == 0) return cudaErrorNotSupported;
-    const int per = (N + ts - 1) / ts;
-    emax = 1;
-    while (emax < per) emax *= 2;
-    qmax = 0;
-    // two slots of [vector | factors] plus two pointer slots of d+1 pointers
-    const int align = 16 / elem;
-    const int slot = round_up(N, align) + round_up(d * n * n, align);
-    vec_pad = slot;  // elements per data slot
-    team_elems = 2 * slot + round_up(2 * (d + 1) * 8 / elem, align);
-    return cudaSuccess;
+    const int N = (int)Nl, F = N / n;
+    const bool forced = tune && tune->team_size > 0;
+    constexpr int kAlign = 16 / (int)sizeof(T);
+    sh.vec_pad = round_up(N, kAlign);
+    // [vector | factors], and in the deterministic mode (n <= 8) a run accumulator of
+    // vec_pad values at the end of the slice
+    sh.team_elems = sh.vec_pad + round_up(d * n * n, kAlign) + (det && n <= 8 ? sh.vec_pad : 0);
+    if (n > 8) {
+        const int ts = elem_team_size(N, 16, forced ? tune->team_size : 0, kGroupedBlock);
+        if (ts == 0) return cudaErrorNotSupported;
+        const int per = (N + ts - 1) / ts;
+        int emax = 1;
+        while (emax < per) emax *= 2;
+        sh.fn = gq_elem_rt_lookup<T, TO>(emax, det);
+        sh.ts = ts;
+        return sh.fn ? cudaSuccess : cudaErrorNotSupported;
+    }
+    const int qcap = (n <= 4) ? 8 : 4;
+    int ts = 8;
+    if (forced) {
+        ts = tune->team_size;
+        while (ts < kGroupedBlock && (F + ts - 1) / ts > qcap) ts *= 2;
+    } else {
+        const int qtarget = (n <= 4 || (n == 6 && sizeof(T) == 8)) ? 4 : 2;
+        while (ts < kGroupedBlock && (long long)ts * qtarget < F) ts *= 2;
+    }
+    if (ts > kGroupedBlock) return cudaErrorNotSupported;
+    const int q = (F + ts - 1) / ts;
+    int qmax = 1;
+    while (qmax < q) qmax *= 2;
+    if (qmax > qcap) return cudaErrorNotSupported;
+    sh.fn = gq_fibre_lookup<T, TO>(n, qmax, det);
+    sh.ts = ts;
+    if (sizeof(T) == 8 && !forced) {
+        const double fibre_util = (double)F / ((double)ts * q);
+        int tse = 8;
+        while (tse < kGroupedBlock && (N + tse - 1) / tse > 4) tse *= 2;
+        const int per = (N + tse - 1) / tse;
+        const double util_e = (double)N / ((double)tse * per);
+        if (per <= 8 && util_e > fibre_util + 0.05) {
+            int emax = 1;
+            while (emax < per) emax *= 2;
+            const GqFn fe = gq_elem_lookup<T, TO>(n, emax, det);
+            if (fe) {
+                sh.fn = fe;
+                sh.ts = tse;
+            }
+        }
+    }
+    return sh.fn ? cudaSuccess : cudaErrorNotSupported;
 }
 
-int grouped_plan_create(GroupedPlan *&out, const kronmult_group *groups, int n_groups, int dtype, int mode,
+int shape_for(int dtype, int d, int n, bool det, const kronmult_tuning *tune, GqShape &sh)
+{
+    return dtype == KRONMULT_DTYPE_F64 ? gq_shape<double, double>(d, n, det, tune, sh)
+                                       : gq_shape<float, float>(d, n, det, tune, sh);
+}
+
+long long pow2_ceil(long long v)
+{
+    long long p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+void destroy_plan(GroupedPlan *pl)
+{
+    if (!pl) return;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev != pl->device) cudaSetDevice(pl->device);
+    for (cudaStream_t s : pl->branches)
+        if (s) cudaStreamDestroy(s);
+    for (cudaEvent_t e : pl->joins)
+        if (e) cudaEventDestroy(e);
+    if (pl->fork) cudaEventDestroy(pl->fork);
+    if (pl->dmem) cudaFree(pl->dmem);
+    if (dev != pl->device) cudaSetDevice(dev);
+    delete pl;
+}
+
+int run_adjoint(int dtype, const kronmult_adjoint_group &g, cudaStream_t st)
+{
+    if (dtype == KRONMULT_DTYPE_F64)
+        return kronmult_batched_adjoint_f64_async(
+            g.matrix_count, g.matrix_size, reinterpret_cast<const double *const *>(g.matrix_list_batched),
+            g.matrix_stride, reinterpret_cast<const double *const *>(g.input_batched),
+            reinterpret_cast<const double *const *>(g.grad_output_batched),
+            reinterpret_cast<double *const *>(g.grad_input_batched),
+            reinterpret_cast<double *const *>(g.grad_matrix_list_batched), g.grad_matrix_stride, g.nb_batch, st,
+            nullptr);
+    return kronmult_batched_adjoint_f32_async(
+        g.matrix_count, g.matrix_size, reinterpret_cast<const float *const *>(g.matrix_list_batched),
+        g.matrix_stride, reinterpret_cast<const float *const *>(g.input_batched),
+        reinterpret_cast<const float *const *>(g.grad_output_batched),
+        reinterpret_cast<float *const *>(g.grad_input_batched),
+        reinterpret_cast<float *const *>(g.grad_matrix_list_batched), g.grad_matrix_stride, g.nb_batch, st, nullptr);
+}
+
+}  // namespace
+
+int grouped_plan_create(GroupedPlan *&out, const kronmult_group *groups, int n_groups,
+                        const kronmult_adjoint_group *adj, int n_adj, int dtype, int mode,
                         const kronmult_tuning *tunings)
 {
     out = nullptr;
-    if (n_groups < 0 || (n_groups > 0 && !groups)) return cudaErrorInvalidValue;
+    if (n_groups < 0 || (n_groups > 0 && !groups) || n_adj < 0 || (n_adj > 0 && !adj)) return cudaErrorInvalidValue;
     if (dtype != KRONMULT_DTYPE_F64 && dtype != KRONMULT_DTYPE_F32) return cudaErrorInvalidValue;
     if (mode != KRONMULT_MODE_ATOMIC && mode != KRONMULT_MODE_DETERMINISTIC) return cudaErrorInvalidValue;
+    const bool det = mode == KRONMULT_MODE_DETERMINISTIC;
     const int elem = dtype == KRONMULT_DTYPE_F64 ? 8 : 4;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return cudaErrorInvalidDevice;
@@ -137,21 +266,7 @@ int grouped_plan_create(GroupedPlan *&out, const kronmult_group *groups, int n_g
     pl->dtype = dtype;
     pl->mode = mode;
     pl->device = dev;
-    std::vector<GroupDesc> descs;
-    std::vector<TeamRange> ranges;
-    struct HostItem {
-        CtaItem ci;
-        double cost;
-    };
-    std::vector<HostItem> hitems;
-    std::vector<long long> perm_all;
-    std::vector<long long> perm_offset;
-    size_t smem_max = 0;
-    const void *fn = grouped_kernel_ptr(dtype, mode);
     int rc = cudaSuccess;
-
-    // first pass: shapes and shared memory, to size the persistent grid
-    std::vector<int> ts(n_groups), qmax(n_groups), te(n_groups), vp(n_groups), tpc(n_groups), em(n_groups);
     for (int g = 0; g < n_groups && rc == cudaSuccess; ++g) {
         const kronmult_group &G = groups[g];
         if (G.matrix_count < 0 || G.matrix_size < 0 || G.nb_batch < 0 ||
@@ -159,7 +274,8 @@ int grouped_plan_create(GroupedPlan *&out, const kronmult_group *groups, int n_g
             rc = cudaErrorInvalidValue;
             break;
         }
-        if (G.nb_batch > 0 && (!G.matrix_list_batched || !G.input_batched || !G.output_batched)) {
+        if (G.nb_batch == 0 || G.matrix_size == 0) continue;  // nothing to add
+        if (!G.matrix_list_batched || !G.input_batched || !G.output_batched) {
             rc = cudaErrorInvalidValue;
             break;
         }
@@ -167,200 +283,164 @@ int grouped_plan_create(GroupedPlan *&out, const kronmult_group *groups, int n_g
         const kronmult_tuning *tp = (tunings && tunings[g].team_size > 0) ? &tunings[g] : nullptr;
         if (!tp && tuning_cache_lookup(G.matrix_count, G.matrix_size, dtype, tt) && tt.team_size <= kGroupedBlock)
             tp = &tt;
-        if (G.nb_batch == 0) {
-            ts[g] = 0;
-            continue;
-        }
-        rc = team_shape(G.matrix_count, G.matrix_size, elem, tp, ts[g], qmax[g], te[g], vp[g], em[g]);
+        GqShape sh;
+        rc = shape_for(dtype, G.matrix_count, G.matrix_size, det, tp, sh);
         if (rc != cudaSuccess) break;
-        tpc[g] = kGroupedBlock / ts[g];
-        while ((size_t)tpc[g] * te[g] * elem > (size_t)di.max_smem_optin && tpc[g] > 1) tpc[g] /= 2;
-        if ((size_t)tpc[g] * te[g] * elem > (size_t)di.max_smem_optin) {
+        const int teams = kGroupedBlock / sh.ts;
+        const size_t smem = (size_t)teams * sh.team_elems * elem;
+        if (smem > (size_t)di.max_smem_optin || !ensure_smem_attr((const void *)sh.fn, smem)) {
             rc = cudaErrorNotSupported;
             break;
         }
-        smem_max = std::max(smem_max, (size_t)tpc[g] * te[g] * elem);
-    }
-    if (rc == cudaSuccess && !ensure_smem_attr(fn, smem_max)) rc = cudaErrorInvalidValue;
-    int per_sm = 1;
-    if (rc == cudaSuccess) {
-        per_sm = std::max(1, occupancy(fn, kGroupedBlock, smem_max));
-        pl->grid = di.sms * per_sm;
-        pl->smem = smem_max;
-        pl->fn = fn;
-    }
-
-    // second pass: entry order, segments, team ranges and CTA items
-    std::vector<const void *> outp;
-    std::map<const void *, int> owner;  // deterministic mode: output vector -> group
-    for (int g = 0; g < n_groups && rc == cudaSuccess; ++g) {
-        const kronmult_group &G = groups[g];
-        GroupDesc gd{};
-        gd.mats = G.matrix_list_batched;
-        gd.in = G.input_batched;
-        gd.out = G.output_batched;
-        gd.perm = nullptr;
-        gd.d = G.matrix_count;
-        gd.n = G.matrix_size;
-        gd.stride = G.matrix_stride;
-        gd.N = (int)pow_ll(G.matrix_size, G.matrix_count);
-        gd.team_size = ts[g];
-        gd.teams_per_cta = tpc[g];
-        gd.team_elems = te[g];
-        gd.vec_pad = vp[g];
-        gd.qmax = qmax[g];
-        gd.emax = em[g];
-        perm_offset.push_back(-1);
-        const long long nb = G.nb_batch;
-        if (nb == 0 || G.matrix_size == 0) {
-            descs.push_back(gd);
-            continue;
-        }
-        // segment boundaries (entry order after the optional sort)
-        std::vector<long long> seg_start;  // start index of each segment in (permuted) order
-        outp.resize((size_t)nb);
-        if (cudaMemcpy(outp.data(), G.output_batched, sizeof(void *) * (size_t)nb, cudaMemcpyDefault) !=
-            cudaSuccess) {
+        GqLaunch L;
+        L.fn = sh.fn;
+        L.smem = smem;
+        L.grid = di.sms * std::max(1, occupancy((const void *)sh.fn, kGroupedBlock, smem));
+        GqArgs &a = L.args;
+        a.mats = G.matrix_list_batched;
+        a.in = G.input_batched;
+        a.out = G.output_batched;
+        a.nb = G.nb_batch;
+        a.d = G.matrix_count;
+        a.n = G.matrix_size;
+        a.stride = G.matrix_stride;
+        a.N = (int)pow_ll(G.matrix_size, G.matrix_count);
+        a.team_size = sh.ts;
+        a.team_elems = sh.team_elems;
+        a.vec_pad = sh.vec_pad;
+        // about four units per resident team (the queue balances the tail), unless tuned
+        const long long teams_total = (long long)L.grid * teams;
+        long long unit = (a.nb + 4 * teams_total - 1) / (4 * teams_total);
+        if (tunings && tunings[g].entries_per_team > 0) unit = tunings[g].entries_per_team;
+        a.unit = std::max(1LL, unit);
+        a.n_units = (a.nb + a.unit - 1) / a.unit;
+        if (a.n_units > (long long)UINT_MAX) {
             rc = cudaErrorInvalidValue;
-            cudaGetLastError();
             break;
         }
-        std::vector<long long> order;
-        if (mode == KRONMULT_MODE_DETERMINISTIC) {
-            for (long long k = 0; k < nb; ++k) {
-                auto ins = owner.emplace(outp[k], g);
-                if (!ins.second && ins.first->second != g) rc = cudaErrorInvalidValue;  // shared across groups
-            }
-            if (rc != cudaSuccess) break;
-            // contiguous already?  (every pointer value occurs in one run)
-            std::vector<const void *> runs;
-            for (long long k = 0; k < nb; ++k)
-                if (k == 0 || outp[k] != outp[k - 1]) runs.push_back(outp[k]);
-            std::vector<const void *> sorted_runs = runs;
-            std::sort(sorted_runs.begin(), sorted_runs.end());
-            const bool contiguous =
-                std::adjacent_find(sorted_runs.begin(), sorted_runs.end()) == sorted_runs.end();
-            if (!contiguous) {
-                order.resize((size_t)nb);
-                std::iota(order.begin(), order.end(), 0LL);
-                std::stable_sort(order.begin(), order.end(),
-                                 [&](long long a, long long b) { return outp[a] < outp[b]; });
-                perm_offset.back() = (long long)perm_all.size();
-                perm_all.insert(perm_all.end(), order.begin(), order.end());
-            }
-            for (long long k = 0; k < nb; ++k) {
-                const void *pk = order.empty() ? outp[k] : outp[order[k]];
-                const void *pp = k == 0 ? nullptr : (order.empty() ? outp[k - 1] : outp[order[k - 1]]);
-                if (k == 0 || pk != pp) seg_start.push_back(k);
-            }
-        } else {
-            for (long long k = 0; k < nb; ++k)
-                if (k == 0 || outp[k] != outp[k - 1]) seg_start.push_back(k);
-        }
-        seg_start.push_back(nb);
-        // entries per team range: about four ranges per resident team, whole segments
-        const long long resident_teams = (long long)pl->grid * tpc[g];
-        long long target = (nb + 4 * resident_teams - 1) / (4 * resident_teams);
-        if (tunings && tunings[g].entries_per_team > 0) target = tunings[g].entries_per_team;
-        if (target < 1) target = 1;
-        std::vector<TeamRange> granges;
-        if (mode == KRONMULT_MODE_DETERMINISTIC) {
-            size_t s = 0;
-            while (s + 1 < seg_start.size()) {
-                const long long b = seg_start[s];
-                long long e = seg_start[s + 1];
-                ++s;
-                while (s + 1 < seg_start.size() && e - b < target) {
-                    e = seg_start[s + 1];
-                    ++s;
-                }
-                granges.push_back({b, e});
-            }
-        } else {
-            for (long long b = 0; b < nb; b += target) granges.push_back({b, std::min(nb, b + target)});
-        }
-        const double unit = (double)gd.d * gd.n * gd.N;  // FMAs per entry
-        for (size_t r0 = 0; r0 < granges.size(); r0 += (size_t)tpc[g]) {
-            const int cnt = (int)std::min<size_t>((size_t)tpc[g], granges.size() - r0);
-            double cost = 0;
-            long long maxlen = 0;
-            for (int t = 0; t < cnt; ++t) maxlen = std::max(maxlen, granges[r0 + t].end - granges[r0 + t].begin);
-            cost = unit * (double)maxlen;
-            hitems.push_back({CtaItem{g, cnt, (long long)(ranges.size() + r0)}, cost});
-        }
-        ranges.insert(ranges.end(), granges.begin(), granges.end());
-        descs.push_back(gd);
+        if (det) L.sort_m = std::max<long long>(kSortLocal, pow2_ceil(a.nb));
+        pl->launches.push_back(L);
+        pl->n_units += a.n_units;
+        pl->grid_max = std::max(pl->grid_max, L.grid);
+        pl->smem_max = std::max(pl->smem_max, smem);
+    }
+    for (int g = 0; g < n_adj && rc == cudaSuccess; ++g) {
+        const kronmult_adjoint_group &A = adj[g];
+        if (A.matrix_count < 0 || A.matrix_size < 0 || A.nb_batch < 0 ||
+            A.matrix_stride < (A.matrix_size > 0 ? A.matrix_size : 1))
+            rc = cudaErrorInvalidValue;
+        else if (A.nb_batch > 0)
+            pl->adjoints.push_back(GqAdjoint{A});
     }
     if (rc != cudaSuccess) {
-        delete pl;
+        destroy_plan(pl);
         return rc;
     }
-    // largest items first: the queue then balances the tail
-    std::stable_sort(hitems.begin(), hitems.end(), [](const HostItem &a, const HostItem &b) { return a.cost > b.cost; });
-    std::vector<CtaItem> items;
-    items.reserve(hitems.size());
-    for (auto &h : hitems) items.push_back(h.ci);
-    pl->n_items = (int)items.size();
-    pl->n_groups = n_groups;
 
-    // device copies: [counters | groups | items | ranges | perm]
+    // device memory: the queue counters, then each deterministic group's sort buffers
     auto align = [](size_t v) { return (v + 255) & ~(size_t)255; };
-    const size_t off_cnt = 0;
-    const size_t off_grp = align(off_cnt + 4 * sizeof(unsigned));
-    const size_t off_itm = align(off_grp + descs.size() * sizeof(GroupDesc));
-    const size_t off_rng = align(off_itm + items.size() * sizeof(CtaItem));
-    const size_t off_prm = align(off_rng + ranges.size() * sizeof(TeamRange));
-    const size_t total = align(off_prm + perm_all.size() * sizeof(long long));
+    size_t total = align(std::max<size_t>(1, pl->launches.size()) * sizeof(unsigned));
+    for (const GqLaunch &L : pl->launches)
+        if (L.sort_m) total += align((size_t)L.sort_m * 8) * 2 + align((size_t)L.args.nb * (L.args.d + 2) * 8);
     if (cudaMalloc(&pl->dmem, total) != cudaSuccess) {
         cudaGetLastError();
-        delete pl;
+        destroy_plan(pl);
         return cudaErrorMemoryAllocation;
     }
-    pl->dmem_bytes = total;
-    char *base = static_cast<char *>(pl->dmem);
-    long long *dperm = reinterpret_cast<long long *>(base + off_prm);
-    for (size_t g = 0; g < descs.size(); ++g)
-        if (perm_offset[g] >= 0) descs[g].perm = dperm + perm_offset[g];
-    pl->counters = reinterpret_cast<unsigned *>(base + off_cnt);
-    pl->groups = reinterpret_cast<GroupDesc *>(base + off_grp);
-    pl->items = reinterpret_cast<CtaItem *>(base + off_itm);
-    pl->ranges = reinterpret_cast<TeamRange *>(base + off_rng);
-    cudaError_t e = cudaMemset(pl->counters, 0, 4 * sizeof(unsigned));
-    if (e == cudaSuccess && !descs.empty())
-        e = cudaMemcpy(pl->groups, descs.data(), descs.size() * sizeof(GroupDesc), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && !items.empty())
-        e = cudaMemcpy(pl->items, items.data(), items.size() * sizeof(CtaItem), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && !ranges.empty())
-        e = cudaMemcpy(pl->ranges, ranges.data(), ranges.size() * sizeof(TeamRange), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && !perm_all.empty())
-        e = cudaMemcpy(dperm, perm_all.data(), perm_all.size() * sizeof(long long), cudaMemcpyHostToDevice);
+    char *p = static_cast<char *>(pl->dmem);
+    pl->counters = reinterpret_cast<unsigned *>(p);
+    p += align(std::max<size_t>(1, pl->launches.size()) * sizeof(unsigned));
+    for (size_t i = 0; i < pl->launches.size(); ++i) {
+        GqLaunch &L = pl->launches[i];
+        L.args.queue = pl->counters + i;
+        if (L.sort_m) {
+            L.keys = reinterpret_cast<unsigned long long *>(p);
+            p += align((size_t)L.sort_m * 8);
+            L.perm = reinterpret_cast<long long *>(p);
+            p += align((size_t)L.sort_m * 8);
+            const long long nb = L.args.nb;
+            L.s_mats = reinterpret_cast<const void **>(p);
+            L.s_in = L.s_mats + nb * L.args.d;
+            L.s_out = const_cast<void **>(L.s_in + nb);
+            p += align((size_t)nb * (L.args.d + 2) * 8);
+            L.mats = L.args.mats;
+            L.in = L.args.in;
+            L.out = L.args.out;
+            L.args.mats = L.s_mats;
+            L.args.in = L.s_in;
+            L.args.out = L.s_out;
+            L.args.keys = L.keys;
+            pl->n_sorted += nb;
+        }
+    }
+    // one branch stream and join event per parallel kernel, one fork event
+    const size_t n_branches = (det ? 0 : pl->launches.size()) + pl->adjoints.size();
+    pl->branches.assign(std::max<size_t>(1, n_branches), nullptr);
+    pl->joins.assign(pl->branches.size(), nullptr);
+    cudaError_t e = cudaEventCreateWithFlags(&pl->fork, cudaEventDisableTiming);
+    for (size_t i = 0; i < pl->branches.size() && e == cudaSuccess; ++i) {
+        e = cudaStreamCreateWithFlags(&pl->branches[i], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&pl->joins[i], cudaEventDisableTiming);
+    }
+    // deterministic mode: order the entries on the device and wait (no copy to the host)
+    if (e == cudaSuccess && det) {
+        for (const GqLaunch &L : pl->launches)
+            gq_group_launch(L.mats, L.in, L.out, L.args.d, L.args.nb, L.sort_m, L.keys, L.perm, L.s_mats, L.s_in,
+                            L.s_out, pl->branches[0]);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaStreamSynchronize(pl->branches[0]);
+    }
     if (e != cudaSuccess) {
-        cudaFree(pl->dmem);
-        delete pl;
+        cudaGetLastError();
+        destroy_plan(pl);
         return e;
     }
-    pl->n_ranges = (long long)ranges.size();
-    pl->n_perm = (long long)perm_all.size();
     out = pl;
     return cudaSuccess;
+}
+
+int grouped_regroup(const GroupedPlan *pl, cudaStream_t st)
+{
+    if (!pl) return cudaErrorInvalidValue;
+    for (const GqLaunch &L : pl->launches)
+        if (L.sort_m)
+            gq_group_launch(L.mats, L.in, L.out, L.args.d, L.args.nb, L.sort_m, L.keys, L.perm, L.s_mats, L.s_in,
+                            L.s_out, st);
+    return (int)cudaGetLastError();
 }
 
 int grouped_run(const GroupedPlan *pl, cudaStream_t st)
 {
     if (!pl) return cudaErrorInvalidValue;
-    if (pl->n_items == 0) return cudaSuccess;
-    cudaError_t e = cudaMemsetAsync(pl->counters, 0, 4 * sizeof(unsigned), st);
+    const bool det = pl->mode == KRONMULT_MODE_DETERMINISTIC;
+    cudaError_t e = cudaSuccess;
+    if (!pl->launches.empty()) e = cudaMemsetAsync(pl->counters, 0, pl->launches.size() * sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
-    if (pl->dtype == KRONMULT_DTYPE_F64) {
-        auto fn = reinterpret_cast<void (*)(const GroupDesc *, const CtaItem *, int, const TeamRange *, unsigned *)>(
-            const_cast<void *>(pl->fn));
-        fn<<<pl->grid, kGroupedBlock, pl->smem, st>>>(pl->groups, pl->items, pl->n_items, pl->ranges, pl->counters);
-    } else {
-        auto fn = reinterpret_cast<void (*)(const GroupDesc *, const CtaItem *, int, const TeamRange *, unsigned *)>(
-            const_cast<void *>(pl->fn));
-        fn<<<pl->grid, kGroupedBlock, pl->smem, st>>>(pl->groups, pl->items, pl->n_items, pl->ranges, pl->counters);
+    auto launch = [&](const GqLaunch &L, cudaStream_t s) {
+        L.fn<<<L.grid, kGroupedBlock, L.smem, s>>>(L.args);
+        return cudaGetLastError();
+    };
+    const size_t n_par = (det ? 0 : pl->launches.size()) + pl->adjoints.size();
+    if (n_par > 0 && (e = cudaEventRecord(pl->fork, st)) != cudaSuccess) return e;
+    size_t b = 0;
+    auto branch = [&](auto &&enqueue) -> cudaError_t {
+        cudaStream_t s = pl->branches[b];
+        cudaError_t r = cudaStreamWaitEvent(s, pl->fork, 0);
+        if (r == cudaSuccess) r = (cudaError_t)enqueue(s);
+        if (r == cudaSuccess) r = cudaEventRecord(pl->joins[b], s);
+        if (r == cudaSuccess) r = cudaStreamWaitEvent(st, pl->joins[b], 0);
+        ++b;
+        return r;
+    };
+    for (const GqLaunch &L : pl->launches) {
+        e = det ? launch(L, st) : branch([&](cudaStream_t s) { return (int)launch(L, s); });
+        if (e != cudaSuccess) return e;
     }
-    return (int)cudaGetLastError();
+    for (const GqAdjoint &A : pl->adjoints) {
+        e = branch([&](cudaStream_t s) { return run_adjoint(pl->dtype, A.g, s); });
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 }  // namespace kgb
@@ -372,9 +452,16 @@ extern "C" {
 int kronmult_grouped_plan_create(kronmult_grouped_plan *plan, const kronmult_group *groups, int n_groups, int dtype,
                                  int mode, const kronmult_tuning *tunings)
 {
+    return kronmult_grouped_plan_create_with_adjoint(plan, groups, n_groups, nullptr, 0, dtype, mode, tunings);
+}
+
+int kronmult_grouped_plan_create_with_adjoint(kronmult_grouped_plan *plan, const kronmult_group *groups,
+                                              int n_groups, const kronmult_adjoint_group *adjoint_groups,
+                                              int n_adjoint, int dtype, int mode, const kronmult_tuning *tunings)
+{
     if (!plan) return cudaErrorInvalidValue;
     GroupedPlan *pl = nullptr;
-    int rc = grouped_plan_create(pl, groups, n_groups, dtype, mode, tunings);
+    const int rc = grouped_plan_create(pl, groups, n_groups, adjoint_groups, n_adjoint, dtype, mode, tunings);
     *plan = reinterpret_cast<kronmult_grouped_plan>(pl);
     return rc;
 }
@@ -384,26 +471,25 @@ int kronmult_grouped_run(kronmult_grouped_plan plan, void *stream)
     return grouped_run(reinterpret_cast<const GroupedPlan *>(plan), (cudaStream_t)stream);
 }
 
+int kronmult_grouped_regroup(kronmult_grouped_plan plan, void *stream)
+{
+    return grouped_regroup(reinterpret_cast<const GroupedPlan *>(plan), (cudaStream_t)stream);
+}
+
 int kronmult_grouped_plan_info(kronmult_grouped_plan plan, long long *info, int n_info)
 {
     auto *pl = reinterpret_cast<const GroupedPlan *>(plan);
     if (!pl || !info) return cudaErrorInvalidValue;
-    const long long v[6] = {pl->grid, kGroupedBlock, (long long)pl->smem, pl->n_items, pl->n_ranges, pl->n_perm};
+    const long long v[6] = {pl->grid_max, kGroupedBlock, (long long)pl->smem_max, pl->n_units,
+                            (long long)(pl->launches.size() + pl->adjoints.size()), pl->n_sorted};
     for (int i = 0; i < n_info && i < 6; ++i) info[i] = v[i];
     return cudaSuccess;
 }
 
 int kronmult_grouped_plan_destroy(kronmult_grouped_plan plan)
 {
-    auto *pl = reinterpret_cast<GroupedPlan *>(plan);
-    if (!pl) return cudaSuccess;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (dev != pl->device) cudaSetDevice(pl->device);
-    cudaError_t e = cudaFree(pl->dmem);
-    if (dev != pl->device) cudaSetDevice(dev);
-    delete pl;
-    return e;
+    destroy_plan(reinterpret_cast<GroupedPlan *>(plan));
+    return cudaSuccess;
 }
 
 }  // extern "C"

@@ -1,44 +1,79 @@
-// Device-side descriptors of the grouped persistent forward.
+// Grouped forward: descriptors shared by the planner (grouped.cu) and the per-group
+// persistent kernels (grouped_kernels.cuh, instantiated in grouped_inst_*.cu).
 #pragma once
+#include <cuda_runtime.h>
+#include <vector>
 #include "fwd_kernels.cuh"
 #include "kronmult_gb300.h"
 
 namespace kgb {
 
-constexpr int kGroupedBlock = 256;  // threads per CTA of the persistent kernel
+constexpr int kGroupedBlock = 256;  // threads per CTA of the persistent kernels
 
-struct GroupDesc {
+// One group's persistent launch: teams pull work units (index u, entries
+// [u*unit, (u+1)*unit)) from `queue` until n_units are taken.  In the deterministic
+// mode the pointer tables are the group's tables gathered in sorted order (entries
+// ordered by output pointer on the device, ties in entry order), `keys` holds the
+// sorted output pointers, and a unit's bounds are moved forward to the next segment
+// start, so that every output vector is summed by exactly one team, in entry order.
+struct GqArgs {
     const void *const *mats;
     const void *const *in;
     void *const *out;
-    const long long *perm;  // entry order (null = identity)
+    const unsigned long long *keys;      // deterministic mode: sorted output pointers
+    unsigned *queue;                     // this group's unit counter (zeroed per run)
+    long long nb, unit, n_units;
     int d, n, stride, N;
-    int team_size, teams_per_cta, team_elems, vec_pad, qmax;
-    int emax;  // > 0: element-mapped team forward with this many outputs per thread
+    int team_size, team_elems, vec_pad;  // vec_pad: offset of the factors in a team's slice
 };
 
-struct CtaItem {             // one queue item: `count` team ranges of one group
-    int group;
-    int count;
-    long long first_range;
+using GqFn = void (*)(const GqArgs);
+
+// Kernel for a group: fibre mapping (compile-time n <= 8, QMAX fibres per thread),
+// element mapping with compile-time n (FP64, EMAX outputs per thread), or element
+// mapping with n at run time (n = 9..16).  Null when no instantiation fits.
+template <typename T, typename TO> GqFn gq_fibre_lookup(int nn, int qmax, bool det);
+template <typename T, typename TO> GqFn gq_elem_lookup(int nn, int emax, bool det);
+template <typename T, typename TO> GqFn gq_elem_rt_lookup(int emax, bool det);
+
+// Device-side grouping of one group's entries by output pointer (deterministic mode):
+// sorts (pointer, entry index) pairs into keys/perm (m >= nb, a power of two >= 2048),
+// then gathers the group's pointer tables in that order into s_mats / s_in / s_out.
+void gq_group_launch(const void *const *mats, const void *const *in, const void *const *out, int d, long long nb,
+                     long long m, unsigned long long *keys, long long *perm, const void **s_mats,
+                     const void **s_in, void **s_out, cudaStream_t st);
+
+struct GqLaunch {
+    GqFn fn = nullptr;
+    int grid = 0;
+    size_t smem = 0;
+    GqArgs args{};
+    // deterministic mode: sort buffers (m = power of two >= nb entries) and the group's
+    // pointer tables in sorted order, which the kernel reads
+    long long sort_m = 0;
+    unsigned long long *keys = nullptr;
+    long long *perm = nullptr;
+    const void **s_mats = nullptr, **s_in = nullptr;
+    void **s_out = nullptr;
+    const void *const *mats = nullptr, *const *in = nullptr, *const *out = nullptr;  // the caller's tables
 };
 
-struct TeamRange {           // entries [begin, end) in the group's (permuted) order
-    long long begin, end;
+struct GqAdjoint {  // one adjoint group, run with the regular adjoint entry point
+    kronmult_adjoint_group g{};
 };
 
 struct GroupedPlan {
-    int dtype = 0, mode = 0, device = 0, n_groups = 0;
-    int grid = 0, n_items = 0;
-    size_t smem = 0;
-    long long n_ranges = 0, n_perm = 0;
-    const void *fn = nullptr;
-    void *dmem = nullptr;  // one allocation holding everything below
-    size_t dmem_bytes = 0;
-    unsigned *counters = nullptr;
-    GroupDesc *groups = nullptr;
-    CtaItem *items = nullptr;
-    TeamRange *ranges = nullptr;
+    int dtype = 0, mode = 0, device = 0;
+    std::vector<GqLaunch> launches;  // forward groups with entries
+    std::vector<GqAdjoint> adjoints;
+    unsigned *counters = nullptr;    // one per launch
+    void *dmem = nullptr;            // counters and sort buffers, one allocation
+    std::vector<cudaStream_t> branches;
+    cudaEvent_t fork = nullptr;
+    std::vector<cudaEvent_t> joins;
+    long long n_units = 0, n_sorted = 0;
+    int grid_max = 0;
+    size_t smem_max = 0;
 };
 
 }  // namespace kgb

@@ -1,0 +1,271 @@
+// Per-group persistent kernels of the grouped forward (no reference counterpart;
+// the reference serves one (d, n) per call, kronmult_gpu/kronmult.cu:173-197).
+//
+// Every group gets a kernel compiled for its own factor size n, with its own
+// register budget, instead of one kernel that takes n at run time: the planner
+// launches one such kernel per group, as parallel branches of one graph (atomic
+// mode) or one after another (deterministic mode).  Each kernel is persistent: a
+// team takes the next work unit from the group's device queue (one atomicAdd by
+// the team's first thread), computes it with the same team forward as the
+// single-call path (entries staged in shared memory, the d modes in place) and takes
+// the next, until the queue is empty.
+#pragma once
+#include "grouped.cuh"
+
+namespace kgb {
+
+// first position >= s that starts a segment of equal output pointers (sorted order)
+__device__ __forceinline__ long long gq_snap(const unsigned long long *keys, long long s, long long nb)
+{
+    while (s > 0 && s < nb && keys[s] == keys[s - 1]) ++s;
+    return s < nb ? s : nb;
+}
+
+// the team's next unit as [b, e) of the group's order; false when the queue is empty
+__device__ __forceinline__ bool gq_next(const GqArgs &a, long long *slot, const Team &tm, long long &b, long long &e)
+{
+    if (tm.rank == 0) *slot = (long long)atomicAdd(a.queue, 1u);
+    tm.sync();
+    const long long u = *slot;
+    tm.sync();
+    if (u >= a.n_units) return false;
+    b = u * a.unit;
+    e = b + a.unit < a.nb ? b + a.unit : a.nb;
+    if (a.keys) {
+        b = gq_snap(a.keys, b, a.nb);
+        e = gq_snap(a.keys, e, a.nb);
+    }
+    return true;
+}
+
+// Adds one entry's result element y into the output.  Atomic mode: with an atomic
+// addition.  Deterministic mode, where the team owns every entry of this output and
+// takes them in entry order: into the run sum `acc` in shared memory (each thread
+// always owns the same elements, so no barrier is needed), and at the run's last
+// entry out = out + sum with one plain read-modify-write.
+template <typename T, typename TO, bool DET>
+__device__ __forceinline__ void gq_add(TO *o, T *acc, int p, T y, bool first, bool last)
+{
+    if constexpr (DET) {
+        const T s = first ? y : acc[p] + y;
+        if (last)
+            o[p] = o[p] + (TO)s;
+        else
+            acc[p] = s;
+    } else {
+        atomic_add<TO>(o + p, (TO)y);
+    }
+}
+
+// One entry, fibre mapping: the body of fwd_single_kernel.
+template <typename T, typename TO, int NN, int QMAX, bool DET>
+__device__ __forceinline__ void gq_entry_fibre(const T *const *mats, const T *const *in, TO *const *out, int d,
+                                               int stride, int N, long long e, T *buf, T *fac, T *acc, bool first,
+                                               bool last, const Team &tm)
+{
+    const int F = N / NN;
+    constexpr bool kSwz = VecSwizzle<T, NN>::on;
+    stage_vector<T, kSwz>(buf, in[e], N, tm);
+    stage_factors<T, NN>(fac, mats + e * d, d, stride, tm);
+    tm.sync();
+    T y[QMAX][NN];
+    for (int i = d - 1; i >= 0; --i) {
+        const T *M = fac + i * NN * NN;
+        mode_team<T, NN, QMAX, kSwz, !FactorInSmem<T, NN>::value>(buf, M, M, F, tm, y);
+        tm.sync();  // every read of buf (and fac) for this mode is done
+        if (i > 0) {
+#pragma unroll
+            for (int q = 0; q < QMAX; ++q) {
+                const int c = tm.rank + q * tm.size;
+                if (c < F) {
+#pragma unroll
+                    for (int r = 0; r < NN; ++r) buf[vec_pos<T, kSwz>(c + r * F)] = y[q][r];
+                }
+            }
+            tm.sync();
+        }
+    }
+    TO *o = out[e];
+#pragma unroll
+    for (int q = 0; q < QMAX; ++q) {
+        const int c = tm.rank + q * tm.size;
+        if (c < F) {
+#pragma unroll
+            for (int r = 0; r < NN; ++r) gq_add<T, TO, DET>(o, acc, c + r * F, y[q][r], first, last);
+        }
+    }
+}
+
+// One entry, element mapping with compile-time n: the body of fwd_single_elem_kernel.
+template <typename T, typename TO, int NN, int EMAX, bool DET>
+__device__ __forceinline__ void gq_entry_elem(const T *const *mats, const T *const *in, TO *const *out, int d,
+                                              int stride, int N, long long e, T *buf, T *fac, T *acc, bool first,
+                                              bool last, const Team &tm)
+{
+    constexpr int P = NN * NN;
+    const int F = N / NN;
+    stage_vector(buf, in[e], N, tm);
+    stage_factors<T, NN>(fac, mats + e * d, d, stride, tm);
+    tm.sync();
+    T y[EMAX];
+    for (int i = d - 1; i >= 0; --i) {
+        const T *M = fac + i * P;
+#pragma unroll
+        for (int j = 0; j < EMAX; ++j) {
+            const int q = tm.rank + j * tm.size;
+            if (q < N) {
+                const int c = q / NN, r = q - c * NN;
+                T x[NN];
+                load_fibre<T, NN>(buf + c * NN, x);
+                T s = T(0);
+#pragma unroll
+                for (int k = 0; k < NN; ++k) s = fma_t<T>(M[r + k * NN], x[k], s);
+                y[j] = s;
+            }
+        }
+        tm.sync();
+        if (i > 0) {
+#pragma unroll
+            for (int j = 0; j < EMAX; ++j) {
+                const int q = tm.rank + j * tm.size;
+                if (q < N) {
+                    const int c = q / NN, r = q - c * NN;
+                    buf[c + r * F] = y[j];
+                }
+            }
+            tm.sync();
+        }
+    }
+    TO *o = out[e];
+#pragma unroll
+    for (int j = 0; j < EMAX; ++j) {
+        const int q = tm.rank + j * tm.size;
+        if (q < N) {
+            const int c = q / NN, r = q - c * NN;
+            gq_add<T, TO, DET>(o, acc, c + r * F, y[j], first, last);
+        }
+    }
+}
+
+// Atomic mode: every entry added into its output with atomics as soon as it is
+// computed.  Deterministic mode: entries in sorted order, runs of one output summed
+// in a shared-memory accumulator (team_elems covers it) and added once.  No run sums
+// in registers: the register footprint of the single-call kernels, 3 FP64 / 4 FP32
+// CTAs of 256 threads per SM.
+template <bool DET>
+__device__ __forceinline__ void gq_run_edges(const GqArgs &a, long long b, long long e, long long ei, bool &first,
+                                             bool &last)
+{
+    if constexpr (DET) {
+        first = ei == b || a.keys[ei - 1] != a.keys[ei];
+        last = ei + 1 == e || a.keys[ei + 1] != a.keys[ei];
+    } else {
+        first = last = true;
+    }
+}
+
+template <typename T, typename TO, int NN, int QMAX, bool DET>
+__global__ void __launch_bounds__(kGroupedBlock, sizeof(T) == 8 ? 3 : 4) gq_fibre_kernel(const GqArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ long long s_unit[kGroupedBlock / 8];
+    const Team tm(a.team_size);
+    T *buf = reinterpret_cast<T *>(smem_raw) + (size_t)tm.id * a.team_elems;
+    T *fac = buf + a.vec_pad;
+    T *acc = buf + (a.team_elems - a.vec_pad);  // deterministic mode: the slice's last vec_pad values
+    const T *const *mats = reinterpret_cast<const T *const *>(a.mats);
+    const T *const *in = reinterpret_cast<const T *const *>(a.in);
+    TO *const *out = reinterpret_cast<TO *const *>(a.out);
+    long long b, e;
+    while (gq_next(a, &s_unit[tm.id], tm, b, e))
+        for (long long ei = b; ei < e; ++ei) {
+            bool first, last;
+            gq_run_edges<DET>(a, b, e, ei, first, last);
+            gq_entry_fibre<T, TO, NN, QMAX, DET>(mats, in, out, a.d, a.stride, a.N, ei, buf, fac, acc, first, last,
+                                                 tm);
+        }
+}
+
+template <typename T, typename TO, int NN, int EMAX, bool DET>
+__global__ void __launch_bounds__(kGroupedBlock, sizeof(T) == 8 ? 3 : 4) gq_elem_kernel(const GqArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ long long s_unit[kGroupedBlock / 8];
+    const Team tm(a.team_size);
+    T *buf = reinterpret_cast<T *>(smem_raw) + (size_t)tm.id * a.team_elems;
+    T *fac = buf + a.vec_pad;
+    T *acc = buf + (a.team_elems - a.vec_pad);
+    const T *const *mats = reinterpret_cast<const T *const *>(a.mats);
+    const T *const *in = reinterpret_cast<const T *const *>(a.in);
+    TO *const *out = reinterpret_cast<TO *const *>(a.out);
+    long long b, e;
+    while (gq_next(a, &s_unit[tm.id], tm, b, e))
+        for (long long ei = b; ei < e; ++ei) {
+            bool first, last;
+            gq_run_edges<DET>(a, b, e, ei, first, last);
+            gq_entry_elem<T, TO, NN, EMAX, DET>(mats, in, out, a.d, a.stride, a.N, ei, buf, fac, acc, first, last,
+                                                tm);
+        }
+}
+
+// n = 9..16: element mapping with n at run time
+template <typename T, typename TO, int EMAX, bool DET>
+__global__ void __launch_bounds__(kGroupedBlock, 2) gq_elem_rt_kernel(const GqArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ long long s_unit[kGroupedBlock / 8];
+    const Team tm(a.team_size);
+    T *buf = reinterpret_cast<T *>(smem_raw) + (size_t)tm.id * a.team_elems;
+    T *fac = buf + a.vec_pad;
+    const T *const *mats = reinterpret_cast<const T *const *>(a.mats);
+    const T *const *in = reinterpret_cast<const T *const *>(a.in);
+    TO *const *out = reinterpret_cast<TO *const *>(a.out);
+    long long b, e;
+    while (gq_next(a, &s_unit[tm.id], tm, b, e))
+        team_forward_elem<T, TO, EMAX, DET>(mats, in, out, nullptr, a.d, a.n, a.stride, a.N, b, e, buf, fac, tm);
+}
+
+}  // namespace kgb
+
+// Lookups of every instantiation for one (T, TO) = (KGB_T, KGB_TO), defined by the
+// including translation unit.  Fibre kernels: QMAX up to 8 for n <= 4, up to 4 above
+// (the planner's cap).  Element kernels with compile-time n: FP64 only (where the
+// pipe is charged per warp instruction, so idle lanes cost time).
+#define KGB_GQ_F1(NN, Q)                                                                                   \
+    case NN * 32 + Q * 2: return gq_fibre_kernel<KGB_T, KGB_TO, NN, Q, false>;                             \
+    case NN * 32 + Q * 2 + 1: return gq_fibre_kernel<KGB_T, KGB_TO, NN, Q, true>;
+#define KGB_GQ_FS(NN) KGB_GQ_F1(NN, 1) KGB_GQ_F1(NN, 2) KGB_GQ_F1(NN, 4) KGB_GQ_F1(NN, 8)
+#define KGB_GQ_FL(NN) KGB_GQ_F1(NN, 1) KGB_GQ_F1(NN, 2) KGB_GQ_F1(NN, 4)
+#define KGB_GQ_E1(NN, E)                                                                                   \
+    case NN * 32 + E * 2: return gq_elem_kernel<KGB_T, KGB_TO, NN, E, false>;                              \
+    case NN * 32 + E * 2 + 1: return gq_elem_kernel<KGB_T, KGB_TO, NN, E, true>;
+#define KGB_GQ_E(NN) KGB_GQ_E1(NN, 1) KGB_GQ_E1(NN, 2) KGB_GQ_E1(NN, 4) KGB_GQ_E1(NN, 8)
+#define KGB_GQ_R(E)                                                                                        \
+    case E * 2: return gq_elem_rt_kernel<KGB_T, KGB_TO, E, false>;                                         \
+    case E * 2 + 1: return gq_elem_rt_kernel<KGB_T, KGB_TO, E, true>;
+
+#define KGB_GQ_LOOKUP_FIBRE_AND_RT                                                                         \
+    template <> GqFn gq_fibre_lookup<KGB_T, KGB_TO>(int nn, int qmax, bool det)                            \
+    {                                                                                                      \
+        switch (nn * 32 + qmax * 2 + (det ? 1 : 0)) {                                                      \
+            KGB_GQ_FS(2) KGB_GQ_FS(3) KGB_GQ_FS(4) KGB_GQ_FL(5) KGB_GQ_FL(6) KGB_GQ_FL(7) KGB_GQ_FL(8)      \
+        default: return nullptr;                                                                           \
+        }                                                                                                  \
+    }                                                                                                      \
+    template <> GqFn gq_elem_rt_lookup<KGB_T, KGB_TO>(int emax, bool det)                                  \
+    {                                                                                                      \
+        switch (emax * 2 + (det ? 1 : 0)) {                                                                \
+            KGB_GQ_R(1) KGB_GQ_R(2) KGB_GQ_R(4) KGB_GQ_R(8) KGB_GQ_R(16)                                    \
+        default: return nullptr;                                                                           \
+        }                                                                                                  \
+    }
+#define KGB_GQ_LOOKUP_ELEM                                                                                 \
+    template <> GqFn gq_elem_lookup<KGB_T, KGB_TO>(int nn, int emax, bool det)                             \
+    {                                                                                                      \
+        switch (nn * 32 + emax * 2 + (det ? 1 : 0)) {                                                      \
+            KGB_GQ_E(2) KGB_GQ_E(3) KGB_GQ_E(4) KGB_GQ_E(5) KGB_GQ_E(6) KGB_GQ_E(7) KGB_GQ_E(8)             \
+        default: return nullptr;                                                                           \
+        }                                                                                                  \
+    }
+#define KGB_GQ_LOOKUP_NO_ELEM                                                                              \
+    template <> GqFn gq_elem_lookup<KGB_T, KGB_TO>(int, int, bool) { return nullptr; }

@@ -1,10 +1,16 @@
-"""Grouped persistent forward and the autotuner, over the C ABI.
+"""Grouped persistent forward (and adjoint) and the autotuner, over the C ABI.
 
 `GroupedPlan([batch, ...], mode)` builds one plan for several DeviceBatch groups
-of different (d, n, fan-in); `plan.run(stream)` enqueues the single persistent
-launch (graph-capturable).  mode "atomic" adds with atomics; "deterministic"
-sums every output's entries in entry order and writes each output once, so the
-result is bitwise reproducible.
+of different (d, n, fan-in); `plan.run(stream)` enqueues, per group, a persistent
+kernel compiled for its n that pulls work from the group's device queue -- in
+parallel graph branches forked from `stream` in the atomic mode, one after another
+in the deterministic mode (graph-capturable either way).  mode "atomic" adds with
+atomics; "deterministic" sums every output's entries in entry order, all in one
+team (the entries are ordered by output pointer on the device at plan creation),
+and adds the sum once, so the result is bitwise reproducible.  `adjoints=[(batch, grad_out,
+grad_in, grad_factors), ...]` adds adjoint groups (api.adjoint's arguments) to the
+same run, as further parallel branches: one replay then runs a forward and its
+backward.
 
 `autotune_forward(d, n, dtype)` times the forward's launch shapes on the GPU and
 stores the fastest in the library's tuning cache, which the planners consult.
@@ -25,23 +31,40 @@ DTYPES = {torch.float64: _lib.KRONMULT_DTYPE_F64, torch.float32: _lib.KRONMULT_D
 
 
 class GroupedPlan:
-    def __init__(self, batches: list[DeviceBatch], mode: str = "atomic", tunings: list[dict] | None = None):
-        if not batches:
+    def __init__(self, batches: list[DeviceBatch], mode: str = "atomic", tunings: list[dict] | None = None,
+                 adjoints: list | None = None):
+        adjoints = list(adjoints or [])
+        if not batches and not adjoints:
             raise ValueError("at least one group is needed")
-        dt = batches[0].inputs.dtype
+        dt = (batches[0] if batches else adjoints[0][0]).inputs.dtype
+        for b in list(batches) + [a[0] for a in adjoints]:
+            if b.inputs.dtype != dt or b.factors.dtype != dt:
+                raise TypeError("all groups must share one dtype (float64 or float32)")
         for b in batches:
-            if b.inputs.dtype != dt or b.outputs.dtype != dt or b.factors.dtype != dt:
+            if b.outputs.dtype != dt:
                 raise TypeError("all groups must share one dtype (float64 or float32)")
         if dt not in DTYPES:
             raise TypeError("grouped forward is defined for float64 and float32")
         self.batches = list(batches)  # keeps the pointer tables alive
         self.mode = mode
-        groups = (_lib.Group * len(batches))()
+        groups = (_lib.Group * max(1, len(batches)))()
         for g, b in zip(groups, batches):
             g.matrix_count, g.matrix_size, g.matrix_stride, g.nb_batch = b.d, b.n, b.stride, b.nb
             g.matrix_list_batched = b.mat_ptrs.data_ptr()
             g.input_batched = b.in_ptrs.data_ptr()
             g.output_batched = b.out_ptrs.data_ptr()
+        adj = (_lib.AdjointGroup * max(1, len(adjoints)))()
+        self._adj_tables = []
+        for a, (b, gout, gin, gfac) in zip(adj, adjoints):
+            tables = _adjoint_tables(b, gout, gin, gfac)
+            self._adj_tables.append((b, gout, gin, gfac) + tables)
+            a.matrix_count, a.matrix_size, a.matrix_stride, a.nb_batch = b.d, b.n, b.stride, b.nb
+            a.matrix_list_batched = b.mat_ptrs.data_ptr()
+            a.input_batched = b.in_ptrs.data_ptr()
+            a.grad_output_batched = tables[0].data_ptr()
+            a.grad_input_batched = None if tables[1] is None else tables[1].data_ptr()
+            a.grad_matrix_list_batched = None if tables[2] is None else tables[2].data_ptr()
+            a.grad_matrix_stride = b.stride
         tp = None
         if tunings is not None:
             arr = (_lib.Tuning * len(batches))()
@@ -53,17 +76,24 @@ class GroupedPlan:
                 a.prefetch = int(t.get("prefetch", 0))
             tp = arr
         self._h = ctypes.c_void_p()
-        st = _lib.lib().kronmult_grouped_plan_create(ctypes.byref(self._h), groups, len(batches), DTYPES[dt],
-                                                      MODES[mode], tp)
+        st = _lib.lib().kronmult_grouped_plan_create_with_adjoint(ctypes.byref(self._h), groups, len(batches), adj,
+                                                                 len(adjoints), DTYPES[dt], MODES[mode], tp)
         _lib.check(st, "kronmult_grouped_plan_create")
+
+    def regroup(self, stream=None) -> None:
+        """Re-run the deterministic mode's device-side ordering (after an output pointer
+        table changed in place); graph-capturable."""
+        _lib.check(_lib.lib().kronmult_grouped_regroup(self._h, _stream_handle(stream)), "kronmult_grouped_regroup")
 
     def run(self, stream=None) -> None:
         _lib.check(_lib.lib().kronmult_grouped_run(self._h, _stream_handle(stream)), "kronmult_grouped_run")
 
     def info(self) -> dict:
+        """grid (largest), block, smem (largest), items (work units of all groups), kernels
+        (per run), sorted (entries ordered on the device, deterministic mode)."""
         v = (ctypes.c_longlong * 6)()
         _lib.check(_lib.lib().kronmult_grouped_plan_info(self._h, v, 6), "kronmult_grouped_plan_info")
-        return dict(zip(("grid", "block", "smem", "items", "ranges", "permuted"), list(v)))
+        return dict(zip(("grid", "block", "smem", "items", "kernels", "sorted"), list(v)))
 
     def close(self) -> None:
         if getattr(self, "_h", None) and self._h.value:
@@ -75,6 +105,29 @@ class GroupedPlan:
             self.close()
         except Exception:
             pass
+
+
+def _adjoint_tables(b: DeviceBatch, grad_out: torch.Tensor, grad_in, grad_fac):
+    """Device pointer tables of an adjoint group (as api.adjoint builds them)."""
+    dev = b.inputs.device
+    es = b.inputs.element_size()
+    N = b.N
+    if grad_out.dtype != b.inputs.dtype or grad_out.shape[1] != N or not grad_out.is_contiguous():
+        raise ValueError("grad_out must be a contiguous (n_out, N) tensor of the batch dtype")
+    gout = grad_out.data_ptr() + b.out_index * (N * es)
+    gin = None
+    if grad_in is not None:
+        if grad_in.shape != b.inputs.shape or grad_in.dtype != b.inputs.dtype or not grad_in.is_contiguous():
+            raise ValueError("grad_in must match the inputs' shape and dtype")
+        k = torch.arange(b.nb, device=dev, dtype=torch.int64)
+        gin = grad_in.data_ptr() + k * (N * es)
+    gmat = None
+    if grad_fac is not None:
+        if grad_fac.shape != b.factors.shape or grad_fac.dtype != b.factors.dtype or not grad_fac.is_contiguous():
+            raise ValueError("grad_factors must match the factors' shape and dtype")
+        i = torch.arange(b.d, device=dev, dtype=torch.int64)
+        gmat = (grad_fac.data_ptr() + (b.fac_index[:, None] * b.d + i[None, :]) * (b.factors.shape[1] * es)).reshape(-1)
+    return gout, gin, gmat
 
 
 def autotune_forward(d: int, n: int, dtype: int = _lib.KRONMULT_DTYPE_F64, nb_sample: int = 0):
@@ -104,7 +157,7 @@ def autotune_grouped(batches: list[DeviceBatch], mode: str = "atomic",
             except _lib.KronmultError:
                 continue
             info = plan.info()
-            shape = (info["block"], info["smem"], info["items"], info["ranges"])
+            shape = (info["block"], info["smem"], info["items"], info["grid"])
             if shape in seen:  # a forced size the planner grew into an already timed shape
                 plan.close()
                 continue

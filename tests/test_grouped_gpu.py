@@ -50,7 +50,7 @@ def test_deterministic_is_bitwise_reproducible(cuda):
     for rep in range(3):
         dbs = device_groups(batches, cuda)
         plan = GroupedPlan(dbs, mode="deterministic")
-        assert plan.info()["permuted"] == sum(b.nb for b in batches)  # outputs were not contiguous
+        assert plan.info()["sorted"] == sum(b.nb for b in batches)  # ordered on the device
         plan.run()
         torch.cuda.synchronize()
         results.append([db.outputs.cpu().numpy().copy() for db in dbs])
@@ -123,17 +123,146 @@ def test_grouped_f32(cuda):
         assert O.rel_l2(db.outputs.cpu().numpy(), O.forward(b)) <= 1e-5
 
 
-def test_shared_output_across_groups_rejected(cuda):
-    import kronmult_gb300 as K
+def test_shared_output_across_groups(cuda):
+    """Two groups adding into the same outputs: the deterministic mode runs the groups
+    one after another, so the sum is right and bitwise the same on every run; the
+    atomic mode is right up to summation order."""
     from kronmult_gb300 import workloads as W
     from kronmult_gb300.grouped import GroupedPlan
 
     b = W.make_batch(2, 4, 4, 2, 3, seed=1)
     db1, db2 = device_groups([b, b], cuda)
-    db2.out_ptrs = db1.out_ptrs.clone()
-    with pytest.raises(K.KronmultError):
-        GroupedPlan([db1, db2], mode="deterministic")
-    GroupedPlan([db1, db2], mode="atomic")  # allowed with atomics
+    db2.out_ptrs = db1.out_ptrs.clone()  # both groups add into db1's outputs
+    want = 2 * O.forward(b)
+    runs = []
+    for mode in ("deterministic", "deterministic", "atomic"):
+        db1.outputs.zero_()
+        GroupedPlan([db1, db2], mode=mode).run()
+        torch.cuda.synchronize()
+        runs.append(db1.outputs.cpu().numpy())
+        assert O.rel_l2(runs[-1], want) <= TOL64
+    assert np.array_equal(runs[0], runs[1])
+
+
+def reference_aliasing(b, distinct):
+    """The reference tests' output map (tests/utils/utils_cpu.h:79-83): entry i < distinct
+    adds into output i, every other entry into output (i*distinct)//nb -- not contiguous."""
+    from kronmult_gb300.workloads import Batch
+
+    idx = np.arange(b.nb, dtype=np.int64)
+    out_index = np.where(idx < distinct, idx, (idx * distinct) // b.nb)
+    return Batch(b.name, b.d, b.n, b.stride, b.block, b.factors, b.inputs, b.out_init[:distinct], b.fac_index,
+                 out_index)
+
+
+@pytest.mark.parametrize("d,n,nb", [(3, 4, 3903), (2, 8, 1000), (4, 6, 700)])
+def test_deterministic_reference_aliasing_bitwise(cuda, d, n, nb):
+    """The reference's non-contiguous aliasing (5 outputs, long runs, entries 0..4 apart
+    from the rest): ordered by output pointer on the device, every output summed by one
+    team in entry order -- the oracle's result, bitwise the same on every plan and run."""
+    from kronmult_gb300 import workloads as W
+    from kronmult_gb300.grouped import GroupedPlan
+
+    b = reference_aliasing(W.make_batch(d, n, n + 3, nb, 1, seed=3900 + d, out_init="normal"), 5)
+    want = O.forward(b)
+    results = []
+    for rep in range(3):
+        db = device_groups([b], cuda)[0]
+        plan = GroupedPlan([db], mode="deterministic", tunings=[{"entries_per_team": 37 + rep}])
+        plan.run()
+        torch.cuda.synchronize()
+        results.append(db.outputs.cpu().numpy())
+        assert O.rel_l2(results[-1], want) <= TOL64
+        plan.close()
+    # the unit size moves where units start, but never splits an output's entries
+    assert np.array_equal(results[0], results[1]) and np.array_equal(results[0], results[2])
+
+
+@pytest.mark.parametrize("captured", [False, True])
+def test_regroup_after_table_change(cuda, captured):
+    """An output pointer table changed in place: kronmult_grouped_regroup (on a stream,
+    optionally captured in the same graph as the run) re-orders the entries on the
+    device and the next run uses the new assignment."""
+    from kronmult_gb300 import workloads as W
+    from kronmult_gb300.grouped import GroupedPlan
+    from kronmult_gb300.workloads import Batch
+
+    b = W.make_batch(3, 5, 6, 40, 6, seed=77)
+    db = device_groups([b], cuda)[0]
+    plan = GroupedPlan([db], mode="deterministic")
+    perm = np.random.Generator(np.random.PCG64(78)).permutation(b.nb)
+    b2 = Batch(b.name, b.d, b.n, b.stride, b.block, b.factors, b.inputs, b.out_init, b.fac_index, b.out_index[perm])
+    new_ptrs = db.outputs.data_ptr() + torch.from_numpy(b2.out_index).to(cuda) * (db.outputs.shape[1] * 8)
+    s = torch.cuda.Stream()
+    db.out_ptrs.copy_(new_ptrs)  # same tensor, new contents
+    torch.cuda.synchronize()
+    db.outputs.zero_()
+    if captured:
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=s):
+            plan.regroup(stream=s)
+            plan.run(stream=s)
+        db.outputs.zero_()
+        g.replay()
+    else:
+        with torch.cuda.stream(s):
+            plan.regroup(stream=s)
+            plan.run(stream=s)
+    torch.cuda.synchronize()
+    assert O.rel_l2(db.outputs.cpu().numpy(), O.forward(b2)) <= TOL64
+
+
+@pytest.mark.parametrize("mode", ["atomic", "deterministic"])
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_runtime_n_groups(cuda, mode, dtype):
+    """n = 9..16 groups (n taken at run time) beside compile-time ones."""
+    from kronmult_gb300 import workloads as W
+    from kronmult_gb300.grouped import GroupedPlan
+
+    batches = [W.make_batch(2, 12, 13, 6, 4, seed=81), W.make_batch(3, 4, 4, 9, 3, seed=82),
+               W.make_batch(2, 9, 9, 5, 5, seed=83)]
+    dbs = device_groups(batches, cuda, dtype=dtype)
+    GroupedPlan(dbs, mode=mode).run()
+    torch.cuda.synchronize()
+    tol = TOL64 if dtype == torch.float64 else 1e-5
+    for b, db in zip(batches, dbs):
+        assert O.rel_l2(db.outputs.cpu().numpy(), O.forward(b)) <= tol
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-13), (torch.float32, 1e-5)])
+def test_forward_and_adjoint_groups_in_one_graph(cuda, dtype, tol):
+    """A plan with a forward group and an adjoint group (the configuration-5 shape with
+    shared factors), captured in one graph: outputs against the oracle, grad_input
+    against the oracle on transposed factors, grad_A against the mode-unfolding formula."""
+    from kronmult_gb300 import DeviceBatch
+    from kronmult_gb300 import workloads as W
+    from kronmult_gb300.grouped import GroupedPlan
+
+    b = W.config5(scale=64 / 2048)
+    g = np.random.Generator(np.random.PCG64(1106)).standard_normal((b.n_out, b.N))
+    db = DeviceBatch.from_host(b, device=cuda, dtype=dtype)
+    gt = torch.from_numpy(g).to(cuda, dtype)
+    gin = torch.zeros_like(db.inputs)
+    gfa = torch.zeros_like(db.factors)
+    plan = GroupedPlan([db], mode="atomic", adjoints=[(db, gt, gin, gfa)])
+    assert plan.info()["kernels"] == 2
+    s = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        plan.run(stream=s)  # warm-up outside the capture
+    torch.cuda.synchronize()
+    with torch.cuda.graph(graph, stream=s):
+        plan.run(stream=s)
+    for t in (db.outputs, gin, gfa):
+        t.zero_()
+    graph.replay()
+    torch.cuda.synchronize()
+    assert O.rel_l2(db.outputs.double().cpu().numpy(), O.forward(b)) <= tol
+    assert O.rel_l2(gin.double().cpu().numpy(), O.forward(O.transposed_batch(b, g))) <= tol
+    n, st = b.n, b.stride
+    gA = gfa.double().cpu().numpy()[:, :n * st].reshape(-1, n, st)[:, :, :n].transpose(0, 2, 1)
+    assert O.rel_l2(gA, O.grad_factors(b, g)) <= tol
+    plan.close()
 
 
 def test_autotune_and_cache(cuda, tmp_path):
