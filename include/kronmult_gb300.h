@@ -140,10 +140,14 @@ int kronmult_batched_adjoint_f32_async(int matrix_count, int matrix_size, const 
  *
  * Deterministic mode: at plan creation every group's entries are ordered by output
  * pointer ON THE DEVICE (a sort of (pointer, entry index) pairs: equal pointers keep
- * their entry order) -- no device-to-host copy; plan creation waits for it.  Every
- * output vector is then owned by one team, which sums its entries in entry order and
- * adds the sum with one plain read-modify-write, out + ((y_0 + y_1) + ...), so the
- * result is bitwise reproducible.  If a group's pointer tables change in place,
+ * their entry order) -- no device-to-host copy; plan creation waits for it.  A
+ * segmented reduction then sums every output's entries in entry order: work units of
+ * consecutive sorted entries sum their runs; an output whose entries lie in one unit
+ * gets one plain read-modify-write, out + ((y_0 + y_1) + ...), and the unit pieces of
+ * an output that spans units are added in order by a second kernel, out + ((s_0 +
+ * s_1) + ...).  The result is bitwise reproducible for a given plan (the grouping of
+ * the sums follows the unit size, tunings[g].entries_per_team, not the scheduling;
+ * for n = 9..16 units are whole outputs).  If a group's pointer tables change in place,
  * kronmult_grouped_regroup re-runs that ordering on a stream (capturable too) before
  * the next run.  Outputs may be shared between groups (the groups run in order).
  *

@@ -129,6 +129,47 @@ void gq_group_launch(const void *const *mats, const void *const *in, const void 
     gq_gather<<<ggrid, 256, 0, st>>>(mats, in, out, d, nb, perm, s_mats, s_in, s_out);
 }
 
+// ---- deterministic mode, second pass ----------------------------------------
+namespace {
+
+// Thread (u, i): when the segment ending unit u continues into unit u+1 and started in
+// unit u, add element i of its partials -- slot 2u+1, then slot 2v of every following
+// unit v it covers, in order -- into the output with one plain read-modify-write.
+template <typename T, typename TO> __global__ void gq_seg_reduce(const GqArgs a)
+{
+    const unsigned long long *k = a.keys;
+    const T *part = reinterpret_cast<const T *>(a.partial);
+    const long long total = a.n_units * (long long)a.N;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const long long u = idx / a.N;
+        const int i = (int)(idx - u * a.N);
+        const long long b = u * a.unit, e = b + a.unit < a.nb ? b + a.unit : a.nb;
+        if (e >= a.nb || k[e - 1] != k[e]) continue;                    // does not continue into u+1
+        if (b > 0 && k[b - 1] == k[b] && k[b] == k[e - 1]) continue;    // started before unit u
+        T s = part[(2 * u + 1) * a.N + i];
+        for (long long v = u + 1;; ++v) {
+            const long long vb = v * a.unit, ve = vb + a.unit < a.nb ? vb + a.unit : a.nb;
+            s += part[(2 * v) * a.N + i];
+            if (!(ve < a.nb && k[vb] == k[ve - 1] && k[ve - 1] == k[ve])) break;  // ends in unit v
+        }
+        TO *o = reinterpret_cast<TO *>(static_cast<uintptr_t>(k[e - 1]));
+        o[i] = o[i] + (TO)s;
+    }
+}
+
+}  // namespace
+
+void gq_seg_reduce_launch(const GqArgs &a, int dtype, cudaStream_t st)
+{
+    const long long total = a.n_units * (long long)a.N;
+    const unsigned grid = (unsigned)std::min<long long>((total + 255) / 256, 8192);
+    if (dtype == KRONMULT_DTYPE_F64)
+        gq_seg_reduce<double, double><<<grid, 256, 0, st>>>(a);
+    else
+        gq_seg_reduce<float, float><<<grid, 256, 0, st>>>(a);
+}
+
 // ---- planning ----------------------------------------------------------------
 
 namespace {
@@ -318,7 +359,10 @@ int grouped_plan_create(GroupedPlan *&out, const kronmult_group *groups, int n_g
             rc = cudaErrorInvalidValue;
             break;
         }
-        if (det) L.sort_m = std::max<long long>(kSortLocal, pow2_ceil(a.nb));
+        if (det) {
+            L.sort_m = std::max<long long>(kSortLocal, pow2_ceil(a.nb));
+            a.snap = G.matrix_size > 8 ? 1 : 0;  // run-time n: whole segments per unit
+        }
         pl->launches.push_back(L);
         pl->n_units += a.n_units;
         pl->grid_max = std::max(pl->grid_max, L.grid);
@@ -341,7 +385,9 @@ int grouped_plan_create(GroupedPlan *&out, const kronmult_group *groups, int n_g
     auto align = [](size_t v) { return (v + 255) & ~(size_t)255; };
     size_t total = align(std::max<size_t>(1, pl->launches.size()) * sizeof(unsigned));
     for (const GqLaunch &L : pl->launches)
-        if (L.sort_m) total += align((size_t)L.sort_m * 8) * 2 + align((size_t)L.args.nb * (L.args.d + 2) * 8);
+        if (L.sort_m)
+            total += align((size_t)L.sort_m * 8) * 2 + align((size_t)L.args.nb * (L.args.d + 2) * 8) +
+                     (L.args.snap ? 0 : align((size_t)2 * L.args.n_units * L.args.N * elem));
     if (cudaMalloc(&pl->dmem, total) != cudaSuccess) {
         cudaGetLastError();
         destroy_plan(pl);
@@ -363,6 +409,10 @@ int grouped_plan_create(GroupedPlan *&out, const kronmult_group *groups, int n_g
             L.s_in = L.s_mats + nb * L.args.d;
             L.s_out = const_cast<void **>(L.s_in + nb);
             p += align((size_t)nb * (L.args.d + 2) * 8);
+            if (!L.args.snap) {
+                L.args.partial = p;
+                p += align((size_t)2 * L.args.n_units * L.args.N * elem);
+            }
             L.mats = L.args.mats;
             L.in = L.args.in;
             L.out = L.args.out;
@@ -433,7 +483,15 @@ int grouped_run(const GroupedPlan *pl, cudaStream_t st)
         return r;
     };
     for (const GqLaunch &L : pl->launches) {
-        e = det ? launch(L, st) : branch([&](cudaStream_t s) { return (int)launch(L, s); });
+        if (det) {
+            e = launch(L, st);
+            if (e == cudaSuccess && L.args.partial) {
+                gq_seg_reduce_launch(L.args, pl->dtype, st);
+                e = cudaGetLastError();
+            }
+        } else {
+            e = branch([&](cudaStream_t s) { return (int)launch(L, s); });
+        }
         if (e != cudaSuccess) return e;
     }
     for (const GqAdjoint &A : pl->adjoints) {

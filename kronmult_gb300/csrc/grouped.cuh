@@ -11,18 +11,27 @@ namespace kgb {
 constexpr int kGroupedBlock = 256;  // threads per CTA of the persistent kernels
 
 // One group's persistent launch: teams pull work units (index u, entries
-// [u*unit, (u+1)*unit)) from `queue` until n_units are taken.  In the deterministic
-// mode the pointer tables are the group's tables gathered in sorted order (entries
-// ordered by output pointer on the device, ties in entry order), `keys` holds the
-// sorted output pointers, and a unit's bounds are moved forward to the next segment
-// start, so that every output vector is summed by exactly one team, in entry order.
+// [u*unit, (u+1)*unit)) from `queue` until n_units are taken.
+//
+// Deterministic mode (a segmented reduction): the pointer tables are the group's
+// tables gathered in sorted order (entries ordered by output pointer on the device,
+// ties in entry order) and `keys` holds the sorted output pointers.  A unit sums each
+// of its runs of equal output pointers in entry order.  A run that is a whole
+// segment (all of that output's entries) is added into the output with one plain
+// read-modify-write; a run that continues from the previous unit goes to partial slot
+// 2u, one that continues into the next unit (and does not come from the previous
+// one) to slot 2u+1 -- N values each.  gq_seg_reduce then adds every segment that
+// crosses unit boundaries: its partials in order, into the output once.  The sums are
+// independent of scheduling: bitwise reproducible for a given unit size.
 struct GqArgs {
     const void *const *mats;
     const void *const *in;
     void *const *out;
     const unsigned long long *keys;      // deterministic mode: sorted output pointers
+    void *partial;                       // deterministic mode: 2 * n_units slots of N compute-type values
     unsigned *queue;                     // this group's unit counter (zeroed per run)
     long long nb, unit, n_units;
+    int snap;  // deterministic mode, n = 9..16: units moved to segment starts instead of partial slots
     int d, n, stride, N;
     int team_size, team_elems, vec_pad;  // vec_pad: offset of the factors in a team's slice
 };
@@ -35,6 +44,9 @@ using GqFn = void (*)(const GqArgs);
 template <typename T, typename TO> GqFn gq_fibre_lookup(int nn, int qmax, bool det);
 template <typename T, typename TO> GqFn gq_elem_lookup(int nn, int emax, bool det);
 template <typename T, typename TO> GqFn gq_elem_rt_lookup(int emax, bool det);
+
+// deterministic mode, after the group's kernel: the segments that cross unit boundaries
+void gq_seg_reduce_launch(const GqArgs &a, int dtype, cudaStream_t st);
 
 // Device-side grouping of one group's entries by output pointer (deterministic mode):
 // sorts (pointer, entry index) pairs into keys/perm (m >= nb, a power of two >= 2048),

@@ -14,13 +14,6 @@
 
 namespace kgb {
 
-// first position >= s that starts a segment of equal output pointers (sorted order)
-__device__ __forceinline__ long long gq_snap(const unsigned long long *keys, long long s, long long nb)
-{
-    while (s > 0 && s < nb && keys[s] == keys[s - 1]) ++s;
-    return s < nb ? s : nb;
-}
-
 // the team's next unit as [b, e) of the group's order; false when the queue is empty
 __device__ __forceinline__ bool gq_next(const GqArgs &a, long long *slot, const Team &tm, long long &b, long long &e)
 {
@@ -31,27 +24,30 @@ __device__ __forceinline__ bool gq_next(const GqArgs &a, long long *slot, const 
     if (u >= a.n_units) return false;
     b = u * a.unit;
     e = b + a.unit < a.nb ? b + a.unit : a.nb;
-    if (a.keys) {
-        b = gq_snap(a.keys, b, a.nb);
-        e = gq_snap(a.keys, e, a.nb);
+    if (a.snap) {  // first positions >= b and >= e that start a segment: whole segments per unit
+        while (b > 0 && b < a.nb && a.keys[b] == a.keys[b - 1]) ++b;
+        while (e > 0 && e < a.nb && a.keys[e] == a.keys[e - 1]) ++e;
     }
     return true;
 }
 
-// Adds one entry's result element y into the output.  Atomic mode: with an atomic
-// addition.  Deterministic mode, where the team owns every entry of this output and
-// takes them in entry order: into the run sum `acc` in shared memory (each thread
-// always owns the same elements, so no barrier is needed), and at the run's last
-// entry out = out + sum with one plain read-modify-write.
+// Adds one entry's result element y (at position p) into the output.  Atomic mode:
+// with an atomic addition.  Deterministic mode, where the team owns this run and
+// takes its entries in entry order: into the run sum `acc` in shared memory (each
+// thread always owns the same elements, so no barrier is needed); at the run's last
+// entry the sum goes into the output with one plain read-modify-write, or into the
+// partial slot `part` when the run crosses a unit boundary.
 template <typename T, typename TO, bool DET>
-__device__ __forceinline__ void gq_add(TO *o, T *acc, int p, T y, bool first, bool last)
+__device__ __forceinline__ void gq_add(TO *o, T *acc, T *part, int p, T y, bool first, bool last)
 {
     if constexpr (DET) {
         const T s = first ? y : acc[p] + y;
-        if (last)
-            o[p] = o[p] + (TO)s;
-        else
+        if (!last)
             acc[p] = s;
+        else if (part)
+            part[p] = s;
+        else
+            o[p] = o[p] + (TO)s;
     } else {
         atomic_add<TO>(o + p, (TO)y);
     }
@@ -60,8 +56,8 @@ __device__ __forceinline__ void gq_add(TO *o, T *acc, int p, T y, bool first, bo
 // One entry, fibre mapping: the body of fwd_single_kernel.
 template <typename T, typename TO, int NN, int QMAX, bool DET>
 __device__ __forceinline__ void gq_entry_fibre(const T *const *mats, const T *const *in, TO *const *out, int d,
-                                               int stride, int N, long long e, T *buf, T *fac, T *acc, bool first,
-                                               bool last, const Team &tm)
+                                               int stride, int N, long long e, T *buf, T *fac, T *acc, T *part,
+                                               bool first, bool last, const Team &tm)
 {
     const int F = N / NN;
     constexpr bool kSwz = VecSwizzle<T, NN>::on;
@@ -91,7 +87,7 @@ __device__ __forceinline__ void gq_entry_fibre(const T *const *mats, const T *co
         const int c = tm.rank + q * tm.size;
         if (c < F) {
 #pragma unroll
-            for (int r = 0; r < NN; ++r) gq_add<T, TO, DET>(o, acc, c + r * F, y[q][r], first, last);
+            for (int r = 0; r < NN; ++r) gq_add<T, TO, DET>(o, acc, part, c + r * F, y[q][r], first, last);
         }
     }
 }
@@ -99,8 +95,8 @@ __device__ __forceinline__ void gq_entry_fibre(const T *const *mats, const T *co
 // One entry, element mapping with compile-time n: the body of fwd_single_elem_kernel.
 template <typename T, typename TO, int NN, int EMAX, bool DET>
 __device__ __forceinline__ void gq_entry_elem(const T *const *mats, const T *const *in, TO *const *out, int d,
-                                              int stride, int N, long long e, T *buf, T *fac, T *acc, bool first,
-                                              bool last, const Team &tm)
+                                              int stride, int N, long long e, T *buf, T *fac, T *acc, T *part,
+                                              bool first, bool last, const Team &tm)
 {
     constexpr int P = NN * NN;
     const int F = N / NN;
@@ -142,7 +138,7 @@ __device__ __forceinline__ void gq_entry_elem(const T *const *mats, const T *con
         const int q = tm.rank + j * tm.size;
         if (q < N) {
             const int c = q / NN, r = q - c * NN;
-            gq_add<T, TO, DET>(o, acc, c + r * F, y[j], first, last);
+            gq_add<T, TO, DET>(o, acc, part, c + r * F, y[j], first, last);
         }
     }
 }
@@ -152,15 +148,27 @@ __device__ __forceinline__ void gq_entry_elem(const T *const *mats, const T *con
 // in a shared-memory accumulator (team_elems covers it) and added once.  No run sums
 // in registers: the register footprint of the single-call kernels, 3 FP64 / 4 FP32
 // CTAs of 256 threads per SM.
-template <bool DET>
-__device__ __forceinline__ void gq_run_edges(const GqArgs &a, long long b, long long e, long long ei, bool &first,
-                                             bool &last)
+// Run edges of entry ei in unit [b, e) (deterministic mode): whether it starts / ends
+// a run of equal output pointers within the unit, and at a run's last entry the
+// partial slot its sum goes to (null: the run is a whole segment, added directly).
+template <typename T, bool DET>
+__device__ __forceinline__ T *gq_run_edges(const GqArgs &a, long long b, long long e, long long ei, long long &rs,
+                                           bool &first, bool &last)
 {
     if constexpr (DET) {
-        first = ei == b || a.keys[ei - 1] != a.keys[ei];
-        last = ei + 1 == e || a.keys[ei + 1] != a.keys[ei];
+        const unsigned long long *k = a.keys;
+        first = ei == b || k[ei - 1] != k[ei];
+        last = ei + 1 == e || k[ei + 1] != k[ei];
+        if (first) rs = ei;
+        if (!last) return nullptr;
+        const bool from_prev = rs == b && b > 0 && k[b - 1] == k[b];
+        const bool into_next = ei + 1 == e && e < a.nb && k[e] == k[ei];
+        if (!from_prev && !into_next) return nullptr;
+        const long long slot = 2 * (b / a.unit) + (from_prev ? 0 : 1);
+        return reinterpret_cast<T *>(a.partial) + slot * (long long)a.N;
     } else {
         first = last = true;
+        return nullptr;
     }
 }
 
@@ -178,12 +186,15 @@ __global__ void __launch_bounds__(kGroupedBlock, sizeof(T) == 8 ? 3 : 4) gq_fibr
     TO *const *out = reinterpret_cast<TO *const *>(a.out);
     long long b, e;
     while (gq_next(a, &s_unit[tm.id], tm, b, e))
+    {
+        long long rs = b;
         for (long long ei = b; ei < e; ++ei) {
             bool first, last;
-            gq_run_edges<DET>(a, b, e, ei, first, last);
-            gq_entry_fibre<T, TO, NN, QMAX, DET>(mats, in, out, a.d, a.stride, a.N, ei, buf, fac, acc, first, last,
-                                                 tm);
+            T *part = gq_run_edges<T, DET>(a, b, e, ei, rs, first, last);
+            gq_entry_fibre<T, TO, NN, QMAX, DET>(mats, in, out, a.d, a.stride, a.N, ei, buf, fac, acc, part, first,
+                                                 last, tm);
         }
+    }
 }
 
 template <typename T, typename TO, int NN, int EMAX, bool DET>
@@ -200,12 +211,15 @@ __global__ void __launch_bounds__(kGroupedBlock, sizeof(T) == 8 ? 3 : 4) gq_elem
     TO *const *out = reinterpret_cast<TO *const *>(a.out);
     long long b, e;
     while (gq_next(a, &s_unit[tm.id], tm, b, e))
+    {
+        long long rs = b;
         for (long long ei = b; ei < e; ++ei) {
             bool first, last;
-            gq_run_edges<DET>(a, b, e, ei, first, last);
-            gq_entry_elem<T, TO, NN, EMAX, DET>(mats, in, out, a.d, a.stride, a.N, ei, buf, fac, acc, first, last,
-                                                tm);
+            T *part = gq_run_edges<T, DET>(a, b, e, ei, rs, first, last);
+            gq_entry_elem<T, TO, NN, EMAX, DET>(mats, in, out, a.d, a.stride, a.N, ei, buf, fac, acc, part, first,
+                                                last, tm);
         }
+    }
 }
 
 // n = 9..16: element mapping with n at run time

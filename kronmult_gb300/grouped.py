@@ -5,9 +5,10 @@ of different (d, n, fan-in); `plan.run(stream)` enqueues, per group, a persisten
 kernel compiled for its n that pulls work from the group's device queue -- in
 parallel graph branches forked from `stream` in the atomic mode, one after another
 in the deterministic mode (graph-capturable either way).  mode "atomic" adds with
-atomics; "deterministic" sums every output's entries in entry order, all in one
-team (the entries are ordered by output pointer on the device at plan creation),
-and adds the sum once, so the result is bitwise reproducible.  `adjoints=[(batch, grad_out,
+atomics; "deterministic" orders the entries by output pointer on the device at
+plan creation and sums every output's entries in entry order with a segmented
+reduction (units of consecutive sorted entries, then the pieces of outputs that
+span units in order), so the result is bitwise reproducible for a given plan.  `adjoints=[(batch, grad_out,
 grad_in, grad_factors), ...]` adds adjoint groups (api.adjoint's arguments) to the
 same run, as further parallel branches: one replay then runs a forward and its
 backward.
