@@ -426,6 +426,40 @@ def suite(args):
         line.update(extra or {})
         print(json.dumps(line), flush=True)
 
+    # FP64 arithmetic on this GPU: FMA pipe, FP64 tensor cores (DMMA), INT8 tensor cores,
+    # and the lower bound of an FP64 emulation by 8-bit integer slices (Ozaki scheme) on
+    # the configuration-2 workload, against the double-float kernel measured below
+    if args.only == "fp64":
+        dm, i8 = ctypes.c_double(0), ctypes.c_double(0)
+        _lib.check(lib.kronmult_diag_fp64_mma_gflops(ctypes.byref(dm)), "kronmult_diag_fp64_mma_gflops")
+        _lib.check(lib.kronmult_diag_int8_mma_tops(ctypes.byref(i8)), "kronmult_diag_int8_mma_tops")
+        b = W.config2(scale=sc)
+        # two modes fused into one n^2 x n^2 contraction (K = 16): d/2 fused modes per entry
+        fused_modes = b.d // 2
+        elements = fused_modes * b.N * b.nb  # element-mode products, each split and recombined
+        db = DeviceBatch.from_host(b, device=dev)
+        from kronmult_gb300.api import forward_f64_emulated
+
+        df_ms = _timed(lambda: forward_f64_emulated(db, stream=st), st, reps)
+        native_ms = _timed(lambda: db.forward(stream=st), st, reps)
+        del db
+        torch.cuda.empty_cache()
+        rows = []
+        for slices in (6, 7, 8):
+            ew = ctypes.c_double(0)
+            _lib.check(lib.kronmult_diag_ozaki_elementwise_ms(elements, slices, ctypes.byref(ew)),
+                       "kronmult_diag_ozaki_elementwise_ms")
+            # triangular slice products (i + j < slices), each a K = n^2 int8 contraction
+            int8_ops = slices * (slices + 1) / 2 * 2.0 * (b.n * b.n) * elements
+            mma_ms = int8_ops / (i8.value * 1e12) * 1e3
+            rows.append({"slices": slices, "bits": 8 * slices - 1, "elementwise_ms": ew.value,
+                         "int8_mma_ms_at_measured_rate": mma_ms, "lower_bound_ms": ew.value + mma_ms})
+        print(json.dumps({"suite": "fp64_arithmetic", "fp64_fma_gflops": fp64_peak, "fp64_mma_gflops": dm.value,
+                          "int8_mma_tops": i8.value, "workload": "fwd_d6_n4_b36864",
+                          "element_mode_products": elements, "native_fp64_ms": native_ms,
+                          "double_float_ms": df_ms, "ozaki": rows}), flush=True)
+        return
+
     # C1, C2: plain forward
     for cname, fn in (("c1", W.config1), ("c2", W.config2)):
         if not want(cname):

@@ -270,6 +270,16 @@ int kronmult_diag_wait_selftest(int *code);
  * reference counterpart).  Allocates and synchronises; not for use in a graph. */
 int kronmult_diag_fp64_fma_gflops(double *gflops);
 
+/* Diagnostics: measured FP64 tensor-core (mma.sync f64) throughput in GFLOP/s and INT8
+ * tensor-core (mma.sync s8) throughput in TOPS of the current GPU; and the time in ms
+ * of the per-element work that an FP64 emulation by 8-bit integer slices on tensor
+ * cores (the Ozaki scheme) needs outside the tensor cores on `elements` element-mode
+ * products with `slices` slices (4..8): fixed-point scaling, splitting, recombination.
+ * No reference counterpart.  Allocate and synchronise; not for use in a graph. */
+int kronmult_diag_fp64_mma_gflops(double *gflops);
+int kronmult_diag_int8_mma_tops(double *tops);
+int kronmult_diag_ozaki_elementwise_ms(long long elements, int slices, double *ms);
+
 /*
  * FP64-accurate forward in emulated arithmetic (no reference counterpart): FP64
  * factors, inputs and outputs; every mode product in double-float (pairs of FP32,

@@ -98,6 +98,9 @@ SIGNATURES = {
     "kronmult_batched_f64_emulated_async": (_i, [_i, _i, _vp, _i, _vp, _vp, _vp, _i, _vp]),
     "kronmult_batched_f64_noalloc": (_i, [_i, _i, _vp, _i, _vp, _vp, _i, _vp]),
     "kronmult_diag_fp64_fma_gflops": (_i, [ctypes.POINTER(ctypes.c_double)]),
+    "kronmult_diag_fp64_mma_gflops": (_i, [ctypes.POINTER(ctypes.c_double)]),
+    "kronmult_diag_int8_mma_tops": (_i, [ctypes.POINTER(ctypes.c_double)]),
+    "kronmult_diag_ozaki_elementwise_ms": (_i, [ctypes.c_longlong, _i, ctypes.POINTER(ctypes.c_double)]),
     "kronmult_pow_int": (ctypes.c_longlong, [_i, _i]),
     "kronmult_error_string": (ctypes.c_char_p, [_i]),
     "kronmult_abi_version": (_i, []),

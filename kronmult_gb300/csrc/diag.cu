@@ -61,3 +61,201 @@ extern "C" int kronmult_diag_fp64_fma_gflops(double *gflops)
     *gflops = flops / (best * 1e-3) / 1e9;
     return cudaSuccess;
 }
+
+// ---------------------------------------------------------------------------
+// Diagnostics behind the choice of FP64 arithmetic (no reference counterpart).
+//
+// kronmult_diag_fp64_mma_gflops: FP64 tensor-core (DMMA) throughput, from warps that
+// issue independent mma.sync m8n8k4 f64 instructions out of registers.
+// kronmult_diag_int8_mma_tops: INT8 tensor-core throughput, mma.sync m16n8k32 s8 -> s32.
+// kronmult_diag_ozaki_elementwise_ms: the per-element work that an FP64 emulation by
+// integer slices on tensor cores (the Ozaki scheme: error-free splitting of each
+// operand into fixed-point 8-bit slices, integer products accumulated exactly, the
+// slice levels recombined into FP64 -- Ozaki, Ogita and Oishi, Numer. Algorithms 2012)
+// has to do outside the tensor cores for every element of every mode product: scale
+// to fixed point, split into `slices` digits, and recombine `slices` levels of integer
+// sums into FP64.  The kernel does exactly that work per element (one FP64 read and
+// one FP64 write, everything else in registers) and no tensor-core work, so its time
+// is a lower bound for the scheme on that many element-mode-products.
+namespace {
+
+__global__ void dmma_rate_kernel(double *out, int iters)
+{
+    const double a = 1.0 + 1e-9 * threadIdx.x, b = 1.0 - 1e-9 * threadIdx.x;
+    double c[8][2];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) c[j][0] = c[j][1] = j;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};"
+                         : "+d"(c[j][0]), "+d"(c[j][1])
+                         : "d"(a), "d"(b));
+    }
+    double s = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) s += c[j][0] + c[j][1];
+    if (s == 1234.5678) out[0] = s;  // keeps the accumulators live
+}
+
+__global__ void imma_rate_kernel(int *out, int iters)
+{
+    const unsigned a = 0x01010101u * (threadIdx.x & 7), b = 0x02020202u;
+    int c[8][4];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) c[j][0] = c[j][1] = c[j][2] = c[j][3] = j;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            asm volatile(
+                "mma.sync.aligned.m16n8k32.row.col.s32.s8.s8.s32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+                "{%0, %1, %2, %3};"
+                : "+r"(c[j][0]), "+r"(c[j][1]), "+r"(c[j][2]), "+r"(c[j][3])
+                : "r"(a), "r"(a), "r"(a), "r"(a), "r"(b), "r"(b));
+    }
+    int s = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) s += c[j][0] + c[j][1] + c[j][2] + c[j][3];
+    if (s == 123456789) out[0] = s;
+}
+
+// one element: FP64 -> fixed point (shared scale), `slices` signed 8-bit digits, a
+// level sum per digit (a stand-in for the exact integer products of that level,
+// which the tensor cores would deliver), levels recombined with shifts into an
+// integer and converted back to FP64
+template <int S> __global__ void ozaki_elementwise_kernel(const double *x, double *y, long long n, double scale)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const long long q = __double2ll_rn(x[i] * scale);
+        int dig[S];
+#pragma unroll
+        for (int l = 0; l < S; ++l) dig[l] = (int)(signed char)(q >> (8 * (S - 1 - l)));
+        long long acc = 0;
+#pragma unroll
+        for (int l = 0; l < S; ++l) acc = (acc << 8) + (long long)dig[l] * dig[S - 1 - l];
+        y[i] = __ll2double_rn(acc) * (1.0 / scale);
+    }
+}
+
+struct DiagTimer {
+    cudaStream_t st = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    DiagTimer()
+    {
+        cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+    }
+    ~DiagTimer()
+    {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cudaStreamDestroy(st);
+    }
+    template <typename F> float best_ms(F &&launch, int reps)
+    {
+        launch();  // warm-up
+        float best = 1e30f;
+        for (int r = 0; r < reps; ++r) {
+            cudaEventRecord(e0, st);
+            launch();
+            cudaEventRecord(e1, st);
+            cudaEventSynchronize(e1);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best) best = ms;
+        }
+        return best;
+    }
+};
+
+int sm_count(int *sms)
+{
+    int dev = 0;
+    cudaError_t rc = cudaGetDevice(&dev);
+    if (rc != cudaSuccess) return rc;
+    return cudaDeviceGetAttribute(sms, cudaDevAttrMultiProcessorCount, dev);
+}
+
+}  // namespace
+
+extern "C" int kronmult_diag_fp64_mma_gflops(double *gflops)
+{
+    if (!gflops) return cudaErrorInvalidValue;
+    int sms = 0;
+    cudaError_t rc = (cudaError_t)sm_count(&sms);
+    if (rc != cudaSuccess) return rc;
+    double *out = nullptr;
+    if ((rc = cudaMalloc(&out, sizeof(double))) != cudaSuccess) return rc;
+    const int blocks = sms * 4, threads = 256, iters = 400;
+    float ms;
+    {
+        DiagTimer t;
+        ms = t.best_ms([&] { dmma_rate_kernel<<<blocks, threads, 0, t.st>>>(out, iters); }, 3);
+    }
+    rc = cudaGetLastError();
+    cudaFree(out);
+    if (rc != cudaSuccess) return rc;
+    const double flops = 512.0 * 8 * iters * ((double)blocks * threads / 32);  // per warp: 8 chains x iters x 512
+    *gflops = flops / (ms * 1e-3) / 1e9;
+    return cudaSuccess;
+}
+
+extern "C" int kronmult_diag_int8_mma_tops(double *tops)
+{
+    if (!tops) return cudaErrorInvalidValue;
+    int sms = 0;
+    cudaError_t rc = (cudaError_t)sm_count(&sms);
+    if (rc != cudaSuccess) return rc;
+    int *out = nullptr;
+    if ((rc = cudaMalloc(&out, sizeof(int))) != cudaSuccess) return rc;
+    const int blocks = sms * 4, threads = 256, iters = 2000;
+    float ms;
+    {
+        DiagTimer t;
+        ms = t.best_ms([&] { imma_rate_kernel<<<blocks, threads, 0, t.st>>>(out, iters); }, 3);
+    }
+    rc = cudaGetLastError();
+    cudaFree(out);
+    if (rc != cudaSuccess) return rc;
+    const double ops = 8192.0 * 8 * iters * ((double)blocks * threads / 32);
+    *tops = ops / (ms * 1e-3) / 1e12;
+    return cudaSuccess;
+}
+
+extern "C" int kronmult_diag_ozaki_elementwise_ms(long long elements, int slices, double *ms)
+{
+    if (!ms || elements <= 0 || slices < 4 || slices > 8) return cudaErrorInvalidValue;
+    double *x = nullptr, *y = nullptr;
+    cudaError_t rc = cudaMalloc(&x, (size_t)elements * sizeof(double));
+    if (rc != cudaSuccess) return rc;
+    if ((rc = cudaMalloc(&y, (size_t)elements * sizeof(double))) != cudaSuccess) {
+        cudaFree(x);
+        return rc;
+    }
+    cudaMemset(x, 0x3f, (size_t)elements * sizeof(double));  // finite values near 0.5
+    int sms = 0;
+    sm_count(&sms);
+    const unsigned grid = (unsigned)sms * 8;
+    const double scale = 0x1p52;
+    float best;
+    {
+        DiagTimer t;
+        auto launch = [&] {
+            switch (slices) {
+            case 4: ozaki_elementwise_kernel<4><<<grid, 256, 0, t.st>>>(x, y, elements, scale); break;
+            case 5: ozaki_elementwise_kernel<5><<<grid, 256, 0, t.st>>>(x, y, elements, scale); break;
+            case 6: ozaki_elementwise_kernel<6><<<grid, 256, 0, t.st>>>(x, y, elements, scale); break;
+            case 7: ozaki_elementwise_kernel<7><<<grid, 256, 0, t.st>>>(x, y, elements, scale); break;
+            default: ozaki_elementwise_kernel<8><<<grid, 256, 0, t.st>>>(x, y, elements, scale); break;
+            }
+        };
+        best = t.best_ms(launch, 3);
+    }
+    rc = cudaGetLastError();
+    cudaFree(x);
+    cudaFree(y);
+    if (rc != cudaSuccess) return rc;
+    *ms = best;
+    return cudaSuccess;
+}
