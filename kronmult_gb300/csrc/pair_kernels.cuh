@@ -201,29 +201,64 @@ __device__ __forceinline__ void team_forward_pairs(const float *const *mats, con
                         x[1][0] = v.z;
                         x[1][1] = v.w;
                     }
-                    // mode i on b, in place row by row
+                    if constexpr (NN == 4) {
+                        // factor columns as 16-byte broadcast loads, FMAs in packed FP32
+                        // pairs over the output index (each half the scalar k-ascending
+                        // FMA chain from 0: the same bits)
+                        const f2 zero2 = f2_pack(0.f, 0.f);
+                        // mode i on b, in place row by row; column b of M1 as rows (0,1), (2,3)
 #pragma unroll
-                    for (int a = 0; a < NN; ++a) {
-                        float t[NN];
+                        for (int a = 0; a < 4; ++a) {
+                            f2 t0 = zero2, t1 = zero2;
+#pragma unroll
+                            for (int b = 0; b < 4; ++b) {
+                                const float4 u = *reinterpret_cast<const float4 *>(M1 + 4 * b);
+                                const f2 xb = f2_pack(x[a][b], x[a][b]);
+                                t0 = f2_fma(f2_pack(u.x, u.y), xb, t0);
+                                t1 = f2_fma(f2_pack(u.z, u.w), xb, t1);
+                            }
+                            f2_unpack(t0, x[a][0], x[a][1]);
+                            f2_unpack(t1, x[a][2], x[a][3]);
+                        }
+                        // mode i-1 on a, column by column
+#pragma unroll
+                        for (int rb = 0; rb < 4; ++rb) {
+                            f2 t0 = zero2, t1 = zero2;
+#pragma unroll
+                            for (int a = 0; a < 4; ++a) {
+                                const float4 w = *reinterpret_cast<const float4 *>(M0 + 4 * a);
+                                const f2 xa = f2_pack(x[a][rb], x[a][rb]);
+                                t0 = f2_fma(f2_pack(w.x, w.y), xa, t0);
+                                t1 = f2_fma(f2_pack(w.z, w.w), xa, t1);
+                            }
+                            f2_unpack(t0, z[q][rb], z[q][rb + 4]);
+                            f2_unpack(t1, z[q][rb + 8], z[q][rb + 12]);
+                        }
+                    } else {
+                        // mode i on b, in place row by row
+#pragma unroll
+                        for (int a = 0; a < NN; ++a) {
+                            float t[NN];
+#pragma unroll
+                            for (int rb = 0; rb < NN; ++rb) {
+                                float s = 0.f;
+#pragma unroll
+                                for (int b = 0; b < NN; ++b) s = fmaf(M1[rb + b * NN], x[a][b], s);
+                                t[rb] = s;
+                            }
+#pragma unroll
+                            for (int rb = 0; rb < NN; ++rb) x[a][rb] = t[rb];
+                        }
+                        // mode i-1 on a, column by column
 #pragma unroll
                         for (int rb = 0; rb < NN; ++rb) {
-                            float s = 0.f;
 #pragma unroll
-                            for (int b = 0; b < NN; ++b) s = fmaf(M1[rb + b * NN], x[a][b], s);
-                            t[rb] = s;
-                        }
+                            for (int ra = 0; ra < NN; ++ra) {
+                                float s = 0.f;
 #pragma unroll
-                        for (int rb = 0; rb < NN; ++rb) x[a][rb] = t[rb];
-                    }
-                    // mode i-1 on a, column by column
-#pragma unroll
-                    for (int rb = 0; rb < NN; ++rb) {
-#pragma unroll
-                        for (int ra = 0; ra < NN; ++ra) {
-                            float s = 0.f;
-#pragma unroll
-                            for (int a = 0; a < NN; ++a) s = fmaf(M0[ra + a * NN], x[a][rb], s);
-                            z[q][rb + NN * ra] = s;
+                                for (int a = 0; a < NN; ++a) s = fmaf(M0[ra + a * NN], x[a][rb], s);
+                                z[q][rb + NN * ra] = s;
+                            }
                         }
                     }
                 }
