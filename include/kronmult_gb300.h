@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define KRONMULT_GB300_VERSION 1
+#define KRONMULT_GB300_VERSION 2 /* 2: kronmult_tuning.fp64_path */
 
 /* Compute modes for the FP32-storage entry points. */
 #define KRONMULT_COMPUTE_FP32 0 /* FP32 FMA on CUDA cores */
@@ -62,6 +62,11 @@ typedef struct kronmult_tuning {
     int prefetch;         /* 0 = automatic, 1 = one staging slot, 2 = copy the next entry asynchronously,
                              3 = as 2 with modes ping-ponging between vector buffers (n x n factors
                              over 128 bytes) */
+    int fp64_path;        /* FP64 forward kernel family: 0 = automatic (the FP64 tensor path for
+                             n = 16, the FP64 FMA pipe otherwise), 1 = FP64 FMA pipe, 2 = FP64
+                             tensor path (mma m8n8k4; n = 6, 7, 8, 16), 3 / 4 = FMA pipe with whole
+                             fibres / one output element per thread (n <= 8).  All give bitwise
+                             the same k-ascending FMA chains. */
 } kronmult_tuning;
 
 /*

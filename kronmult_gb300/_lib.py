@@ -20,7 +20,7 @@ class Tuning(ctypes.Structure):
     """Mirror of `kronmult_tuning`: launch-shape override, zero = heuristic."""
 
     _fields_ = [("team_size", ctypes.c_int), ("ctas_per_sm", ctypes.c_int), ("entries_per_team", ctypes.c_int),
-                ("prefetch", ctypes.c_int)]
+                ("prefetch", ctypes.c_int), ("fp64_path", ctypes.c_int)]
 
 
 class Group(ctypes.Structure):
@@ -145,5 +145,5 @@ def tuning_ptr(t: Tuning | dict | None):
         return None
     if isinstance(t, dict):
         t = Tuning(int(t.get("team_size", 0)), int(t.get("ctas_per_sm", 0)), int(t.get("entries_per_team", 0)),
-                   int(t.get("prefetch", 0)))
+                   int(t.get("prefetch", 0)), int(t.get("fp64_path", 0)))
     return ctypes.byref(t)

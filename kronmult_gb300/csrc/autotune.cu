@@ -87,6 +87,27 @@ int autotune_impl(int d, int n, int dtype, int nb_sample, kronmult_tuning *best,
         fill_uniform<T><<<1024, 256, 0, st>>>(x, (size_t)nb * N, 2);
         cudaMemsetAsync(y, 0, sizeof(TO) * (size_t)n_out * N, st);
         build_tables<T, TO><<<256, 256, 0, st>>>(mats, in, out, fac, x, y, nb, d, n, N, fan);
+        // FP64 n with a tensor-path kernel: that plan is a candidate too (its own shape)
+        if (sizeof(T) == 8 && dmma_has_n(n)) {
+            kronmult_tuning t{0, 0, 0, 0, 2};
+            FwdPlan<T, TO> pl;
+            if (plan_forward<T, TO>(pl, d, n, mats, n, in, out, nullptr, nb, &t) == cudaSuccess && pl.smem_path) {
+                launch_plan<T, TO>(pl, st);
+                for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {
+                    cudaEventRecord(e0, st);
+                    launch_plan<T, TO>(pl, st);
+                    cudaEventRecord(e1, st);
+                    if ((e = cudaEventSynchronize(e1)) != cudaSuccess) break;
+                    float ms = 0;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    if (ms < best_t) {
+                        best_t = ms;
+                        best_tune = t;
+                        found = true;
+                    }
+                }
+            }
+        }
         const int F = N / n;
         const int qcap = n <= 4 ? 8 : 4;
         for (int ts = 8; ts <= 512 && e == cudaSuccess; ts *= 2) {
@@ -99,7 +120,7 @@ int autotune_impl(int d, int n, int dtype, int nb_sample, kronmult_tuning *best,
             for (int cand = 0; cand < 3 * nstage; ++cand) {
                 const int ept = (cand % 3 == 0) ? 0 : (cand % 3 == 1 ? 2 : 8);
                 const int stage = cand / 3;  // 0, 1, 2 -> prefetch 2, 1, 3
-                kronmult_tuning t{ts, 0, ept, stage == 0 ? 2 : (stage == 1 ? 1 : 3)};
+                kronmult_tuning t{ts, 0, ept, stage == 0 ? 2 : (stage == 1 ? 1 : 3), sizeof(T) == 8 ? 1 : 0};
                 FwdPlan<T, TO> pl;
                 if (plan_forward<T, TO>(pl, d, n, mats, n, in, out, nullptr, nb, &t) != cudaSuccess) continue;
                 if (!pl.smem_path) continue;
@@ -188,7 +209,8 @@ int kronmult_tuning_cache_get(int matrix_count, int matrix_size, int dtype, kron
 
 int kronmult_tuning_cache_set(int matrix_count, int matrix_size, int dtype, const kronmult_tuning *t)
 {
-    if (!t || t->team_size < 0 || t->ctas_per_sm < 0 || t->entries_per_team < 0 || t->prefetch < 0 || t->prefetch > 3)
+    if (!t || t->team_size < 0 || t->ctas_per_sm < 0 || t->entries_per_team < 0 || t->prefetch < 0 || t->prefetch > 3 ||
+        t->fp64_path < 0 || t->fp64_path > 4)
         return cudaErrorInvalidValue;
     tuning_cache_store(matrix_count, matrix_size, dtype, *t);
     return cudaSuccess;
@@ -207,11 +229,12 @@ int kronmult_tuning_cache_save(const char *path)
     FILE *f = std::fopen(path, "w");
     if (!f) return cudaErrorInvalidValue;
     std::lock_guard<std::mutex> lk(g_mu);
-    std::fprintf(f, "# kronmult_gb300 tuning cache v2: sms d n dtype team_size ctas_per_sm entries_per_team prefetch\n");
+    std::fprintf(f, "# kronmult_gb300 tuning cache v3: sms d n dtype team_size ctas_per_sm entries_per_team prefetch "
+                    "fp64_path\n");
     for (auto &kv : g_cache)
-        std::fprintf(f, "%d %d %d %d %d %d %d %d\n", std::get<0>(kv.first), std::get<1>(kv.first), std::get<2>(kv.first),
-                     std::get<3>(kv.first), kv.second.team_size, kv.second.ctas_per_sm, kv.second.entries_per_team,
-                     kv.second.prefetch);
+        std::fprintf(f, "%d %d %d %d %d %d %d %d %d\n", std::get<0>(kv.first), std::get<1>(kv.first),
+                     std::get<2>(kv.first), std::get<3>(kv.first), kv.second.team_size, kv.second.ctas_per_sm,
+                     kv.second.entries_per_team, kv.second.prefetch, kv.second.fp64_path);
     std::fclose(f);
     return cudaSuccess;
 }
@@ -225,11 +248,12 @@ int kronmult_tuning_cache_load(const char *path)
     std::lock_guard<std::mutex> lk(g_mu);
     while (std::fgets(line, sizeof line, f)) {
         if (line[0] == '#') continue;
-        int v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        const int got = std::sscanf(line, "%d %d %d %d %d %d %d %d", &v[0], &v[1], &v[2], &v[3], &v[4], &v[5], &v[6],
-                                    &v[7]);
-        if (got == 7 || got == 8)
-            g_cache[std::make_tuple(v[0], v[1], v[2], v[3])] = kronmult_tuning{v[4], v[5], v[6], v[7]};
+        int v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        const int got = std::sscanf(line, "%d %d %d %d %d %d %d %d %d", &v[0], &v[1], &v[2], &v[3], &v[4], &v[5],
+                                    &v[6], &v[7], &v[8]);
+        // v2 lines (8 fields) and older (7) load with the automatic FP64 path
+        if (got >= 7 && got <= 9)
+            g_cache[std::make_tuple(v[0], v[1], v[2], v[3])] = kronmult_tuning{v[4], v[5], v[6], v[7], v[8]};
     }
     std::fclose(f);
     return cudaSuccess;

@@ -3,6 +3,7 @@
 #include <climits>
 #include <cstdint>
 #include <mutex>
+#include "dmma_kernels.cuh"
 #include "fwd_kernels.cuh"
 #include "pair_kernels.cuh"
 #include "kronmult_gb300.h"
@@ -72,6 +73,30 @@ inline int elem_team_size(int N, int max_per, int forced, int max_ts)
         }
     }
     return ts;
+}
+
+// Lane use of a mapping in which a team of ts threads covers `items` work items in
+// rounds of ts (item = rank + j * ts), when the FP64 pipe is charged per warp
+// instruction issued: in teams of a warp or more, a warp whose lanes all fall beyond
+// `items` skips the round, so ceil(items / 32) warp rounds issue; sub-warp teams share
+// a warp and each issues ceil(items / ts) rounds.
+inline double lane_use(int items, int ts)
+{
+    if (ts >= 32) return (double)items / (32.0 * ((items + 31) / 32));
+    return (double)items / ((double)ts * ((items + ts - 1) / ts));
+}
+
+// Margin by which the element mapping's lane use must beat the fibre mapping's before
+// the FP64 planners take it (measured: equal lane use left the fibre kernels as fast or
+// up to 16 % faster; d = 6, n = 3, 99 % against 95 %, is the closest case taken).
+constexpr double kElemMargin = 0.03;
+
+// FP64 mapping forced by kronmult_tuning::fp64_path: 3 = whole fibres per thread,
+// 4 = one output element per thread (both on the FMA pipe); 0 otherwise.
+inline int fp64_mapping(const kronmult_tuning *tune)
+{
+    const int p = tune ? tune->fp64_path : 0;
+    return (p == 3 || p == 4) ? p : 0;
 }
 
 // largest power of two <= v (v >= 1)
@@ -173,6 +198,62 @@ bool plan_split(FwdPlan<T, TO> &pl, const DeviceInfo &di)
     return false;
 }
 
+// Whether an FP64 forward of factor size n runs on the FP64 tensor path: forced by
+// tuning->fp64_path == 2, automatic (0) for n = 16 only, where the FMA pipe has only the
+// generic run-time-n kernel (n <= 8 has compile-time-n FMA kernels, and n = 9..15 fill
+// the 8 x 8 MMA tile too poorly: both measured faster on the FMA pipe).
+inline bool dmma_wanted(int n, const kronmult_tuning *tune)
+{
+    const int path = tune ? tune->fp64_path : 0;
+    if (!dmma_has_n(n)) return false;
+    return path == 2 || (path == 0 && n == 16);
+}
+
+// FP64 tensor-path plan (fwd_dmma_kernel): one entry per team of W warps, each warp
+// QT tiles of 8 fibres (W * QT * 8 >= F, at most 8 tiles per warp), the vector and the
+// factors in shared memory.  False where no instantiation or shared-memory size fits.
+template <typename T, typename TO>
+bool plan_dmma(FwdPlan<T, TO> &pl, const DeviceInfo &di, const kronmult_tuning *tune)
+{
+    if constexpr (sizeof(T) != 8 || sizeof(TO) != 8) {
+        return false;
+    } else {
+        FwdArgs<T, TO> &a = pl.args;
+        const int n = a.n, d = a.d, N = a.N;
+        if (d < 1 || !dmma_wanted(n, tune)) return false;
+        const int F = N / n, tiles = (F + 7) / 8;
+        int W = 1;
+        while (W < 8 && W * 8 < tiles) W *= 2;
+        const int per = (tiles + W - 1) / W;
+        int qt = 1;
+        while (qt < per) qt *= 2;
+        const bool full = F % 8 == 0 && tiles == W * qt;
+        DmmaFn fn = fwd_dmma_lookup(n, qt, full);
+        if (!fn) return false;
+        const int vpad = round_up(N, 2), fpad = round_up(d * n * n, 2);
+        const int team_elems = vpad + fpad, ts = 32 * W;
+        int teams = 256 / ts;
+        while (teams > 1 && (size_t)teams * team_elems * sizeof(T) > (size_t)di.max_smem_optin) teams /= 2;
+        const size_t smem = (size_t)teams * team_elems * sizeof(T);
+        if (smem > (size_t)di.max_smem_optin || !ensure_smem_attr((const void *)fn, smem)) return false;
+        const long long grid = (a.nb + teams - 1) / teams;
+        if (grid > INT_MAX) return false;
+        a.team_size = ts;
+        a.teams_per_cta = teams;
+        a.entries_per_team = 1;
+        a.team_elems = team_elems;
+        a.vec_pad = vpad;
+        a.fac_pad = fpad;
+        a.prefetch = 0;
+        pl.fn = (const void *)fn;
+        pl.smem_path = true;
+        pl.grid = dim3((unsigned)grid);
+        pl.block = dim3((unsigned)(teams * ts));
+        pl.smem = smem;
+        return true;
+    }
+}
+
 // Checks arguments and fills a plan.  Returns cudaSuccess, cudaErrorInvalidValue,
 // or cudaErrorNotSupported (vector too long for any path without a workspace).
 template <typename T, typename TO>
@@ -210,6 +291,9 @@ int plan_forward(FwdPlan<T, TO> &pl, int d, int n, const T *const *mats, int str
     a.n = n;
     a.stride = stride;
     a.N = N;
+
+    // ---- FP64 on the tensor path (n = 7, 8, 16 unless tuned otherwise)
+    if (plan_dmma<T, TO>(pl, di, tune)) return cudaSuccess;
 
     // ---- register in-place shared-memory path: 2 <= n <= 8, d >= 1
     if (n >= 2 && n <= 8 && d >= 1) {
@@ -261,13 +345,20 @@ int plan_forward(FwdPlan<T, TO> &pl, int d, int n, const T *const *mats, int str
             // (for odd n the baseline was an element kernel taking n at run time); where
             // the lane use is equal (d = 2, n = 6..8; d = 4, n = 4..6) the fibre kernels were
             // as fast or up to 16 % faster.
-            const double fibre_util = (double)F / ((double)ts * ((F + ts - 1) / ts));
-            if (sizeof(T) == 8 && !(tune && tune->team_size > 0)) {
+            const double fibre_util = lane_use(F, ts);
+            const int fmap = fp64_mapping(tune);
+            if (sizeof(T) == 8 && fmap != 3 && (fmap == 4 || !(tune && tune->team_size > 0))) {
                 int tse = 8;
-                while (tse < 256 && (N + tse - 1) / tse > 4) tse *= 2;
+                if (fmap == 4 && tune->team_size > 0) {
+                    tse = tune->team_size;
+                    while (tse < 256 && (N + tse - 1) / tse > 8) tse *= 2;
+                } else {
+                    while (tse < 256 && (N + tse - 1) / tse > 4) tse *= 2;
+                }
                 const int per = (N + tse - 1) / tse;
-                const double util_e = (double)N / ((double)tse * per);
-                if (per <= 8 && util_e > fibre_util + 0.05) {  // at most 8 elements: no spills
+                const double util_e = lane_use(N, tse);
+                // at most 8 elements per thread: no spills
+                if (tse <= 256 && per <= 8 && (fmap == 4 || util_e > fibre_util + kElemMargin)) {
                     int emax = 1;
                     while (emax < per) emax *= 2;
                     auto fe = fwd_single_elem_lookup<T, TO>(n, emax);
@@ -447,7 +538,23 @@ int plan_forward(FwdPlan<T, TO> &pl, int d, int n, const T *const *mats, int str
     // ---- large vectors: two passes through the workspace (input left intact)
     if (plan_split<T, TO>(pl, di)) return cudaSuccess;
 
-    // ---- larger still: every mode through input/workspace in global memory
+    // ---- larger still: every mode through input/workspace in global memory, FP64
+    // on the tensor path where it is wanted
+    if constexpr (sizeof(T) == 8 && sizeof(TO) == 8) {
+        if (d >= 1 && ws && dmma_wanted(n, tune)) {
+            const size_t smem_s = ((size_t)round_up(n * n, 2) + 2 * (size_t)round_up(N, 2)) * sizeof(T);
+            auto fn = fwd_dmma_global_lookup(n);
+            if (fn && smem_s > (size_t)di.max_smem_optin) {
+                const long long grid = nb < INT_MAX ? nb : INT_MAX;  // one CTA per entry
+                pl.fn = (const void *)fn;
+                pl.smem_path = true;
+                pl.grid = dim3((unsigned)grid);
+                pl.block = dim3(512);
+                pl.smem = 0;
+                return cudaSuccess;
+            }
+        }
+    }
     if (n >= 2 && n <= 8 && d >= 1 && ws) {
         const size_t smem_s = ((size_t)round_up(n * n, 2) + 2 * (size_t)round_up(N, 2)) * sizeof(T);
         if (smem_s > (size_t)di.max_smem_optin) {

@@ -221,13 +221,19 @@ int gq_shape(int d, int n, bool det, const kronmult_tuning *tune, GqShape &sh)
     if (qmax > qcap) return cudaErrorNotSupported;
     sh.fn = gq_fibre_lookup<T, TO>(n, qmax, det);
     sh.ts = ts;
-    if (sizeof(T) == 8 && !forced) {
-        const double fibre_util = (double)F / ((double)ts * q);
+    const int fmap = fp64_mapping(tune);
+    if (sizeof(T) == 8 && fmap != 3 && (fmap == 4 || !forced)) {
+        const double fibre_util = lane_use(F, ts);
         int tse = 8;
-        while (tse < kGroupedBlock && (N + tse - 1) / tse > 4) tse *= 2;
+        if (fmap == 4 && forced) {
+            tse = tune->team_size;
+            while (tse < kGroupedBlock && (N + tse - 1) / tse > 8) tse *= 2;
+        } else {
+            while (tse < kGroupedBlock && (N + tse - 1) / tse > 4) tse *= 2;
+        }
         const int per = (N + tse - 1) / tse;
-        const double util_e = (double)N / ((double)tse * per);
-        if (per <= 8 && util_e > fibre_util + 0.05) {
+        const double util_e = lane_use(N, tse);
+        if (tse <= kGroupedBlock && per <= 8 && (fmap == 4 || util_e > fibre_util + kElemMargin)) {
             int emax = 1;
             while (emax < per) emax *= 2;
             const GqFn fe = gq_elem_lookup<T, TO>(n, emax, det);
@@ -321,7 +327,8 @@ int grouped_plan_create(GroupedPlan *&out, const kronmult_group *groups, int n_g
             break;
         }
         kronmult_tuning tt{};
-        const kronmult_tuning *tp = (tunings && tunings[g].team_size > 0) ? &tunings[g] : nullptr;
+        const kronmult_tuning *tp =
+            (tunings && (tunings[g].team_size > 0 || fp64_mapping(&tunings[g]))) ? &tunings[g] : nullptr;
         if (!tp && tuning_cache_lookup(G.matrix_count, G.matrix_size, dtype, tt) && tt.team_size <= kGroupedBlock)
             tp = &tt;
         GqShape sh;

@@ -75,6 +75,7 @@ class GroupedPlan:
                 a.ctas_per_sm = int(t.get("ctas_per_sm", 0))
                 a.entries_per_team = int(t.get("entries_per_team", 0))
                 a.prefetch = int(t.get("prefetch", 0))
+                a.fp64_path = int(t.get("fp64_path", 0))
             tp = arr
         self._h = ctypes.c_void_p()
         st = _lib.lib().kronmult_grouped_plan_create_with_adjoint(ctypes.byref(self._h), groups, len(batches), adj,
@@ -151,8 +152,12 @@ def autotune_grouped(batches: list[DeviceBatch], mode: str = "atomic",
     for b in batches:
         saved = b.outputs.clone()
         best, best_ms, seen = {}, float("inf"), set()
-        for ts in team_sizes:
+        # FP64: both FMA-pipe mappings (whole fibres, one element per thread) for each size
+        maps = (0, 3, 4) if b.inputs.dtype == torch.float64 and b.n <= 8 else (0,)
+        for ts, fmap in ((t, m) for t in team_sizes for m in maps):
             t = {"team_size": int(ts)} if ts else {}
+            if fmap:
+                t["fp64_path"] = fmap
             try:
                 plan = GroupedPlan([b], mode=mode, tunings=[t])
             except _lib.KronmultError:
@@ -190,12 +195,13 @@ def tuning_cache_get(d: int, n: int, dtype: int = _lib.KRONMULT_DTYPE_F64):
 
 def _as_dict(t) -> dict:
     return {"team_size": t.team_size, "ctas_per_sm": t.ctas_per_sm, "entries_per_team": t.entries_per_team,
-            "prefetch": t.prefetch}
+            "prefetch": t.prefetch, "fp64_path": t.fp64_path}
 
 
 def tuning_cache_set(d: int, n: int, dtype: int, tuning: dict) -> None:
     t = _lib.Tuning(int(tuning.get("team_size", 0)), int(tuning.get("ctas_per_sm", 0)),
-                    int(tuning.get("entries_per_team", 0)), int(tuning.get("prefetch", 0)))
+                    int(tuning.get("entries_per_team", 0)), int(tuning.get("prefetch", 0)),
+                    int(tuning.get("fp64_path", 0)))
     _lib.check(_lib.lib().kronmult_tuning_cache_set(d, n, dtype, ctypes.byref(t)), "kronmult_tuning_cache_set")
 
 

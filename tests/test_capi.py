@@ -111,14 +111,27 @@ def test_tuning_cache_roundtrip_on_host(lib, tmp_path):
     from kronmult_gb300 import grouped as G
 
     G.tuning_cache_clear()
-    G.tuning_cache_set(5, 3, 0, {"team_size": 64, "entries_per_team": 4})
-    assert G.tuning_cache_get(5, 3, 0) == {"team_size": 64, "ctas_per_sm": 0, "entries_per_team": 4, "prefetch": 0}
+    G.tuning_cache_set(5, 3, 0, {"team_size": 64, "entries_per_team": 4, "fp64_path": 4})
+    assert G.tuning_cache_get(5, 3, 0) == {"team_size": 64, "ctas_per_sm": 0, "entries_per_team": 4, "prefetch": 0,
+                                           "fp64_path": 4}
     path = str(tmp_path / "t.txt")
     G.tuning_cache_save(path)
     G.tuning_cache_clear()
     assert G.tuning_cache_get(5, 3, 0) is None
     G.tuning_cache_load(path)
     assert G.tuning_cache_get(5, 3, 0)["team_size"] == 64
+    assert G.tuning_cache_get(5, 3, 0)["fp64_path"] == 4
+    # a cache written before fp64_path existed (8 fields per line) loads with the automatic path
+    lines = [ln.split() for ln in open(path) if not ln.startswith("#")]
+    assert len(lines) == 1 and len(lines[0]) == 9
+    with open(path, "w") as f:
+        f.write("# v2\n" + " ".join(lines[0][:8]) + "\n")
+    G.tuning_cache_clear()
+    G.tuning_cache_load(path)
+    assert G.tuning_cache_get(5, 3, 0)["fp64_path"] == 0
+    G.tuning_cache_clear()
+    with pytest.raises(Exception):
+        G.tuning_cache_set(5, 3, 0, {"fp64_path": 5})
     G.tuning_cache_clear()
 
 
