@@ -546,6 +546,30 @@ def suite(args):
         emit(f"c3_grouped_{mode}_autotuned_graph_f64", groups, ms, 8, 8,
              {"plan": plan.info(), "team_sizes": [t.get("team_size", 0) for t in tunings]})
         plan.close()
+        # FP64 data, mode products in double-float arithmetic on the FP32 pipe
+        with torch.cuda.stream(st):
+            for x in dbs:
+                x.outputs.zero_()
+            plan = G.GroupedPlan(dbs, mode=mode)
+            plan.run(stream=st)
+        torch.cuda.synchronize()
+        native = [x.outputs.clone() for x in dbs]
+        plan.close()
+        plan = G.GroupedPlan(dbs, mode=mode, arithmetic="emulated")
+        with torch.cuda.stream(st):
+            for x in dbs:
+                x.outputs.zero_()
+            plan.run(stream=st)
+        torch.cuda.synchronize()
+        num = sum(float(torch.linalg.norm(x.outputs - y) ** 2) for x, y in zip(dbs, native))
+        den = sum(float(torch.linalg.norm(y) ** 2) for y in native)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=st):
+            plan.run(stream=st)
+        ms = _timed(lambda: graph.replay(), torch.cuda.current_stream(), reps)
+        emit(f"c3_grouped_{mode}_emulated_graph_f64", groups, ms, 8, 8,
+             {"plan": plan.info(), "rel_l2_vs_native_fp64": (num / den) ** 0.5})
+        plan.close()
     del dbs
     torch.cuda.empty_cache()
 

@@ -47,6 +47,9 @@ extern "C" {
 #define KRONMULT_DTYPE_F64 0        /* double factors, inputs and outputs */
 #define KRONMULT_DTYPE_F32 1        /* float factors, inputs and outputs */
 #define KRONMULT_DTYPE_F32_F64OUT 2 /* float factors and inputs, double outputs */
+#define KRONMULT_DTYPE_F64_EMULATED 3 /* grouped plans: double factors, inputs and outputs, mode products in
+                                        double-float arithmetic on the FP32 pipe (as
+                                        kronmult_batched_f64_emulated_async; n = 2..8) */
 
 /* Output modes of the grouped entry point. */
 #define KRONMULT_MODE_ATOMIC 0        /* atomic additions into shared outputs */

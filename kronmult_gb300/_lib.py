@@ -44,6 +44,7 @@ class AdjointGroup(ctypes.Structure):
 KRONMULT_DTYPE_F64 = 0
 KRONMULT_DTYPE_F32 = 1
 KRONMULT_DTYPE_F32_F64OUT = 2
+KRONMULT_DTYPE_F64_EMULATED = 3
 KRONMULT_MODE_ATOMIC = 0
 KRONMULT_MODE_DETERMINISTIC = 1
 KRONMULT_NOALLOC_MAX_ENTRIES = 1048576

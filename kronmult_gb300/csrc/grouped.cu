@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <climits>
 #include <vector>
+#include "df_common.cuh"
 #include "fwd_launch.cuh"
 #include "grouped.cuh"
 #include "tuning.cuh"
@@ -164,7 +165,7 @@ void gq_seg_reduce_launch(const GqArgs &a, int dtype, cudaStream_t st)
 {
     const long long total = a.n_units * (long long)a.N;
     const unsigned grid = (unsigned)std::min<long long>((total + 255) / 256, 8192);
-    if (dtype == KRONMULT_DTYPE_F64)
+    if (dtype == KRONMULT_DTYPE_F64 || dtype == KRONMULT_DTYPE_F64_EMULATED)
         gq_seg_reduce<double, double><<<grid, 256, 0, st>>>(a);
     else
         gq_seg_reduce<float, float><<<grid, 256, 0, st>>>(a);
@@ -233,7 +234,9 @@ int gq_shape(int d, int n, bool det, const kronmult_tuning *tune, GqShape &sh)
         }
         const int per = (N + tse - 1) / tse;
         const double util_e = lane_use(N, tse);
-        if (tse <= kGroupedBlock && per <= 8 && (fmap == 4 || util_e > fibre_util + kElemMargin)) {
+        // ties go to the element mapping here: on C3's groups (d, n) = (2,8), (4,4) its
+        // persistent kernels measured 3-9 % faster at equal lane use
+        if (tse <= kGroupedBlock && per <= 8 && (fmap == 4 || util_e >= fibre_util)) {
             int emax = 1;
             while (emax < per) emax *= 2;
             const GqFn fe = gq_elem_lookup<T, TO>(n, emax, det);
@@ -246,8 +249,32 @@ int gq_shape(int d, int n, bool det, const kronmult_tuning *tune, GqShape &sh)
     return sh.fn ? cudaSuccess : cudaErrorNotSupported;
 }
 
+// Double-float shape: the single-call emulated path's team (whole fibres, at most 4
+// per thread), the slice df_entry wants plus, in deterministic mode, N FP64 run sums.
+int gq_df_shape(int d, int n, bool det, const kronmult_tuning *tune, GqShape &sh)
+{
+    const long long Nl = pow_ll(n, d);
+    if (n < 2 || n > 8 || d < 1 || Nl > (long long)INT_MAX) return cudaErrorNotSupported;
+    const int N = (int)Nl, F = N / n;
+    int qmax = 0;
+    int ts = df_team(F, qmax);
+    if (tune && tune->team_size > 0 && ts) {
+        ts = std::max(ts, std::min(tune->team_size, kGroupedBlock));
+        const int q = (F + ts - 1) / ts;
+        qmax = 1;
+        while (qmax < q) qmax *= 2;
+    }
+    if (!ts || ts > kGroupedBlock) return cudaErrorNotSupported;
+    sh.vec_pad = round_up(N, 4);
+    sh.team_elems = df_slice_floats(d, n, sh.vec_pad) + (det ? 2 * round_up(N, 2) : 0);
+    sh.fn = gq_df_lookup(n, qmax, det);
+    sh.ts = ts;
+    return sh.fn ? cudaSuccess : cudaErrorNotSupported;
+}
+
 int shape_for(int dtype, int d, int n, bool det, const kronmult_tuning *tune, GqShape &sh)
 {
+    if (dtype == KRONMULT_DTYPE_F64_EMULATED) return gq_df_shape(d, n, det, tune, sh);
     return dtype == KRONMULT_DTYPE_F64 ? gq_shape<double, double>(d, n, det, tune, sh)
                                        : gq_shape<float, float>(d, n, det, tune, sh);
 }
@@ -277,7 +304,7 @@ void destroy_plan(GroupedPlan *pl)
 
 int run_adjoint(int dtype, const kronmult_adjoint_group &g, cudaStream_t st)
 {
-    if (dtype == KRONMULT_DTYPE_F64)
+    if (dtype != KRONMULT_DTYPE_F32)  // FP64 data (native or emulated forward): the FP64 adjoint
         return kronmult_batched_adjoint_f64_async(
             g.matrix_count, g.matrix_size, reinterpret_cast<const double *const *>(g.matrix_list_batched),
             g.matrix_stride, reinterpret_cast<const double *const *>(g.input_batched),
@@ -301,10 +328,14 @@ int grouped_plan_create(GroupedPlan *&out, const kronmult_group *groups, int n_g
 {
     out = nullptr;
     if (n_groups < 0 || (n_groups > 0 && !groups) || n_adj < 0 || (n_adj > 0 && !adj)) return cudaErrorInvalidValue;
-    if (dtype != KRONMULT_DTYPE_F64 && dtype != KRONMULT_DTYPE_F32) return cudaErrorInvalidValue;
+    if (dtype != KRONMULT_DTYPE_F64 && dtype != KRONMULT_DTYPE_F32 && dtype != KRONMULT_DTYPE_F64_EMULATED)
+        return cudaErrorInvalidValue;
     if (mode != KRONMULT_MODE_ATOMIC && mode != KRONMULT_MODE_DETERMINISTIC) return cudaErrorInvalidValue;
     const bool det = mode == KRONMULT_MODE_DETERMINISTIC;
+    // bytes of a shared-memory element (floats for the double-float kernels) and of a
+    // run sum / partial-slot value (FP64 for both FP64 forms)
     const int elem = dtype == KRONMULT_DTYPE_F64 ? 8 : 4;
+    const int acc_elem = dtype == KRONMULT_DTYPE_F32 ? 4 : 8;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return cudaErrorInvalidDevice;
     const DeviceInfo &di = device_info(dev);
@@ -356,9 +387,14 @@ int grouped_plan_create(GroupedPlan *&out, const kronmult_group *groups, int n_g
         a.team_size = sh.ts;
         a.team_elems = sh.team_elems;
         a.vec_pad = sh.vec_pad;
-        // about four units per resident team (the queue balances the tail), unless tuned
+        // Unit size, unless tuned: FP64 atomic mode takes one entry per unit (the queue
+        // then evens out the tail to one entry; measured 2-6 % faster than four units per
+        // team on C3's groups, where an entry is 1-15 us of FP64 work); otherwise about
+        // four units per resident team (deterministic mode sums runs within a unit, and
+        // single entries measured up to 14 % slower there).
         const long long teams_total = (long long)L.grid * teams;
         long long unit = (a.nb + 4 * teams_total - 1) / (4 * teams_total);
+        if (dtype != KRONMULT_DTYPE_F32 && !det) unit = 1;
         if (tunings && tunings[g].entries_per_team > 0) unit = tunings[g].entries_per_team;
         a.unit = std::max(1LL, unit);
         a.n_units = (a.nb + a.unit - 1) / a.unit;
@@ -394,7 +430,7 @@ int grouped_plan_create(GroupedPlan *&out, const kronmult_group *groups, int n_g
     for (const GqLaunch &L : pl->launches)
         if (L.sort_m)
             total += align((size_t)L.sort_m * 8) * 2 + align((size_t)L.args.nb * (L.args.d + 2) * 8) +
-                     (L.args.snap ? 0 : align((size_t)2 * L.args.n_units * L.args.N * elem));
+                     (L.args.snap ? 0 : align((size_t)2 * L.args.n_units * L.args.N * acc_elem));
     if (cudaMalloc(&pl->dmem, total) != cudaSuccess) {
         cudaGetLastError();
         destroy_plan(pl);
@@ -418,7 +454,7 @@ int grouped_plan_create(GroupedPlan *&out, const kronmult_group *groups, int n_g
             p += align((size_t)nb * (L.args.d + 2) * 8);
             if (!L.args.snap) {
                 L.args.partial = p;
-                p += align((size_t)2 * L.args.n_units * L.args.N * elem);
+                p += align((size_t)2 * L.args.n_units * L.args.N * acc_elem);
             }
             L.mats = L.args.mats;
             L.in = L.args.in;

@@ -45,6 +45,10 @@ template <typename T, typename TO> GqFn gq_fibre_lookup(int nn, int qmax, bool d
 template <typename T, typename TO> GqFn gq_elem_lookup(int nn, int emax, bool det);
 template <typename T, typename TO> GqFn gq_elem_rt_lookup(int emax, bool det);
 
+// Double-float kernel for a group (FP64 data, FP32-pipe arithmetic; n = 2..8, QMAX
+// fibres per thread up to 4).  Null when no instantiation fits.
+GqFn gq_df_lookup(int nn, int qmax, bool det);
+
 // deterministic mode, after the group's kernel: the segments that cross unit boundaries
 void gq_seg_reduce_launch(const GqArgs &a, int dtype, cudaStream_t st);
 

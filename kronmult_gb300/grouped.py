@@ -33,8 +33,13 @@ DTYPES = {torch.float64: _lib.KRONMULT_DTYPE_F64, torch.float32: _lib.KRONMULT_D
 
 class GroupedPlan:
     def __init__(self, batches: list[DeviceBatch], mode: str = "atomic", tunings: list[dict] | None = None,
-                 adjoints: list | None = None):
+                 adjoints: list | None = None, arithmetic: str = "native"):
+        """arithmetic "emulated" (float64 groups, n <= 8): the forward groups' mode products
+        in double-float arithmetic on the FP32 pipe (KRONMULT_DTYPE_F64_EMULATED; relative
+        error ~1e-14 instead of the native FMA chains' bits); adjoint groups stay native."""
         adjoints = list(adjoints or [])
+        if arithmetic not in ("native", "emulated"):
+            raise ValueError("arithmetic must be 'native' or 'emulated'")
         if not batches and not adjoints:
             raise ValueError("at least one group is needed")
         dt = (batches[0] if batches else adjoints[0][0]).inputs.dtype
@@ -46,6 +51,11 @@ class GroupedPlan:
                 raise TypeError("all groups must share one dtype (float64 or float32)")
         if dt not in DTYPES:
             raise TypeError("grouped forward is defined for float64 and float32")
+        code = DTYPES[dt]
+        if arithmetic == "emulated":
+            if dt != torch.float64:
+                raise TypeError("emulated arithmetic is defined for float64 groups")
+            code = _lib.KRONMULT_DTYPE_F64_EMULATED
         self.batches = list(batches)  # keeps the pointer tables alive
         self.mode = mode
         groups = (_lib.Group * max(1, len(batches)))()
@@ -79,7 +89,7 @@ class GroupedPlan:
             tp = arr
         self._h = ctypes.c_void_p()
         st = _lib.lib().kronmult_grouped_plan_create_with_adjoint(ctypes.byref(self._h), groups, len(batches), adj,
-                                                                 len(adjoints), DTYPES[dt], MODES[mode], tp)
+                                                                 len(adjoints), code, MODES[mode], tp)
         _lib.check(st, "kronmult_grouped_plan_create")
 
     def regroup(self, stream=None) -> None:

@@ -308,3 +308,64 @@ def test_autotune_grouped_tunings_give_correct_results(cuda):
     for db, b in zip(dbs, groups):
         assert O.rel_l2(db.outputs.cpu().numpy(), O.forward(b)) <= 1e-13
     plan.close()
+
+
+@pytest.mark.parametrize("mode", ["atomic", "deterministic"])
+def test_emulated_groups(cuda, mode):
+    """arithmetic="emulated": every group's mode products in double-float arithmetic on
+    the FP32 pipe; FP64-accurate (relative L2 <= 1e-13 against the oracle), scrambled
+    outputs, the deterministic mode bitwise the same on every replay."""
+    from kronmult_gb300 import workloads as W
+    from kronmult_gb300.grouped import GroupedPlan
+
+    batches = [scrambled(b, 40 + i) for i, b in enumerate(W.config3(scale=0.03))]
+    dbs = device_groups(batches, cuda)
+    plan = GroupedPlan(dbs, mode=mode, arithmetic="emulated")
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        plan.run(stream=s)
+    torch.cuda.synchronize()
+    first = [db.outputs.clone() for db in dbs]
+    for b, got in zip(batches, first):
+        assert O.rel_l2(got.cpu().numpy(), O.forward(b)) <= TOL64
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        plan.run(stream=s)
+    for db in dbs:
+        db.outputs.zero_()
+    g.replay()
+    torch.cuda.synchronize()
+    for b, db, f in zip(batches, dbs, first):
+        assert O.rel_l2(db.outputs.cpu().numpy(), O.forward(b)) <= TOL64
+        if mode == "deterministic":
+            assert torch.equal(db.outputs, f)
+    plan.close()
+
+
+def test_emulated_groups_with_adjoint_and_limits(cuda):
+    """An emulated forward group and a native FP64 adjoint group in one plan; n > 8 and
+    float32 groups are refused for the emulated arithmetic."""
+    from kronmult_gb300 import _lib, adjoint
+    from kronmult_gb300 import workloads as W
+    from kronmult_gb300.grouped import GroupedPlan
+
+    b = W.make_batch(3, 6, 6, 16, 4, seed=4100)
+    db, dba = device_groups([b, b], cuda)
+    g = torch.from_numpy(np.random.Generator(np.random.PCG64(4101)).standard_normal((b.n_out, b.N))).to(cuda)
+    gin = torch.zeros_like(dba.inputs)
+    gfa = torch.zeros_like(dba.factors)
+    plan = GroupedPlan([db], mode="atomic", adjoints=[(dba, g, gin, gfa)], arithmetic="emulated")
+    plan.run()
+    torch.cuda.synchronize()
+    assert O.rel_l2(db.outputs.cpu().numpy(), O.forward(b)) <= TOL64
+    gin2 = torch.zeros_like(dba.inputs)
+    gfa2 = torch.zeros_like(dba.factors)
+    adjoint(dba, g, gin2, gfa2)
+    torch.cuda.synchronize()
+    assert O.rel_l2(gin.cpu().numpy(), gin2.cpu().numpy()) <= TOL64
+    plan.close()
+    big = device_groups([W.make_batch(2, 9, 9, 4, 1, seed=4102)], cuda)
+    with pytest.raises(_lib.KronmultError):
+        GroupedPlan(big, arithmetic="emulated")
+    with pytest.raises(TypeError):
+        GroupedPlan(device_groups([b], cuda, dtype=torch.float32), arithmetic="emulated")
