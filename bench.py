@@ -458,6 +458,19 @@ def suite(args):
                           "int8_mma_tops": i8.value, "workload": "fwd_d6_n4_b36864",
                           "element_mode_products": elements, "native_fp64_ms": native_ms,
                           "double_float_ms": df_ms, "ozaki": rows}), flush=True)
+        # the forward on the FP64 tensor path (mma m8n8k4) against the FMA-pipe kernels,
+        # same batches (bitwise the same outputs with one output per entry)
+        for d, n, n_out, fan in ((2, 8, 14000, 8), (4, 8, 512, 8), (3, 7, 3000, 8), (2, 16, 2000, 8),
+                                 (3, 16, 128, 8), (6, 8, 400, 1)):
+            b = W.make_batch(d, n, n, max(1, int(round(n_out * sc))), fan, seed=77)
+            db = DeviceBatch.from_host(b, device=dev, with_workspace=n ** d * 8 > 200000)
+            row = {"suite": "fp64_tensor_path", "d": d, "n": n, "nb": b.nb}
+            for name, t in (("fma_pipe", {"fp64_path": 1}), ("tensor_path", {"fp64_path": 2})):
+                ms = _timed(lambda: db.forward(stream=st, tuning=t), st, reps)
+                row[name] = {"ms": ms, "gflops": b.flops() / ms / 1e6}
+            print(json.dumps(row), flush=True)
+            del db
+            torch.cuda.empty_cache()
         return
 
     # C1, C2: plain forward

@@ -243,6 +243,7 @@ int gq_shape(int d, int n, bool det, const kronmult_tuning *tune, GqShape &sh)
             if (fe) {
                 sh.fn = fe;
                 sh.ts = tse;
+                sh.team_elems += sh.vec_pad;  // the element kernels ping-pong between two vectors
             }
         }
     }

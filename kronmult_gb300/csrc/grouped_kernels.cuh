@@ -92,18 +92,25 @@ __device__ __forceinline__ void gq_entry_fibre(const T *const *mats, const T *co
     }
 }
 
-// One entry, element mapping with compile-time n: the body of fwd_single_elem_kernel.
+// One entry, element mapping with compile-time n (the arithmetic of
+// fwd_single_elem_kernel), ping-ponging between two vector buffers: each output element
+// goes to the other buffer as soon as it is computed (the last mode's straight into the
+// output), so a mode ends with one barrier and no results wait in registers.  The
+// barrier before staging keeps the previous entry's last reads ahead of the new copy.
 template <typename T, typename TO, int NN, int EMAX, bool DET>
 __device__ __forceinline__ void gq_entry_elem(const T *const *mats, const T *const *in, TO *const *out, int d,
-                                              int stride, int N, long long e, T *buf, T *fac, T *acc, T *part,
-                                              bool first, bool last, const Team &tm)
+                                              int stride, int N, long long e, T *buf, T *buf2, T *fac, T *acc,
+                                              T *part, bool first, bool last, const Team &tm)
 {
     constexpr int P = NN * NN;
     const int F = N / NN;
+    tm.sync();
     stage_vector(buf, in[e], N, tm);
     stage_factors<T, NN>(fac, mats + e * d, d, stride, tm);
     tm.sync();
-    T y[EMAX];
+    TO *o = out[e];
+    const T *src = buf;
+    T *dst = buf2;
     for (int i = d - 1; i >= 0; --i) {
         const T *M = fac + i * P;
 #pragma unroll
@@ -112,33 +119,21 @@ __device__ __forceinline__ void gq_entry_elem(const T *const *mats, const T *con
             if (q < N) {
                 const int c = q / NN, r = q - c * NN;
                 T x[NN];
-                load_fibre<T, NN>(buf + c * NN, x);
+                load_fibre<T, NN>(src + c * NN, x);
                 T s = T(0);
 #pragma unroll
                 for (int k = 0; k < NN; ++k) s = fma_t<T>(M[r + k * NN], x[k], s);
-                y[j] = s;
+                if (i > 0)
+                    dst[c + r * F] = s;
+                else
+                    gq_add<T, TO, DET>(o, acc, part, c + r * F, s, first, last);
             }
         }
-        tm.sync();
         if (i > 0) {
-#pragma unroll
-            for (int j = 0; j < EMAX; ++j) {
-                const int q = tm.rank + j * tm.size;
-                if (q < N) {
-                    const int c = q / NN, r = q - c * NN;
-                    buf[c + r * F] = y[j];
-                }
-            }
-            tm.sync();
-        }
-    }
-    TO *o = out[e];
-#pragma unroll
-    for (int j = 0; j < EMAX; ++j) {
-        const int q = tm.rank + j * tm.size;
-        if (q < N) {
-            const int c = q / NN, r = q - c * NN;
-            gq_add<T, TO, DET>(o, acc, part, c + r * F, y[j], first, last);
+            tm.sync();  // the mode's results are complete in dst, its reads of src done
+            T *t = const_cast<T *>(src);
+            src = dst;
+            dst = t;
         }
     }
 }
@@ -197,14 +192,19 @@ __global__ void __launch_bounds__(kGroupedBlock, sizeof(T) == 8 ? 3 : 4) gq_fibr
     }
 }
 
+// FP64 atomic mode with at most 4 outputs per thread fits 48 registers without spills:
+// 5 CTAs of 256 threads per SM (more warps to keep the FP64 pipe fed across barriers).
 template <typename T, typename TO, int NN, int EMAX, bool DET>
-__global__ void __launch_bounds__(kGroupedBlock, sizeof(T) == 8 ? 3 : 4) gq_elem_kernel(const GqArgs a)
+__global__ void __launch_bounds__(kGroupedBlock, sizeof(T) == 8 ? (DET || EMAX > 4 ? 3 : 5) : 4)
+    gq_elem_kernel(const GqArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ long long s_unit[kGroupedBlock / 8];
     const Team tm(a.team_size);
+    // slice: [vector | second vector | factors | run sums (deterministic mode)]
     T *buf = reinterpret_cast<T *>(smem_raw) + (size_t)tm.id * a.team_elems;
-    T *fac = buf + a.vec_pad;
+    T *buf2 = buf + a.vec_pad;
+    T *fac = buf + 2 * a.vec_pad;
     T *acc = buf + (a.team_elems - a.vec_pad);
     const T *const *mats = reinterpret_cast<const T *const *>(a.mats);
     const T *const *in = reinterpret_cast<const T *const *>(a.in);
@@ -216,8 +216,8 @@ __global__ void __launch_bounds__(kGroupedBlock, sizeof(T) == 8 ? 3 : 4) gq_elem
         for (long long ei = b; ei < e; ++ei) {
             bool first, last;
             T *part = gq_run_edges<T, DET>(a, b, e, ei, rs, first, last);
-            gq_entry_elem<T, TO, NN, EMAX, DET>(mats, in, out, a.d, a.stride, a.N, ei, buf, fac, acc, part, first,
-                                                last, tm);
+            gq_entry_elem<T, TO, NN, EMAX, DET>(mats, in, out, a.d, a.stride, a.N, ei, buf, buf2, fac, acc, part,
+                                                first, last, tm);
         }
     }
 }
