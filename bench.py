@@ -458,6 +458,14 @@ def suite(args):
                           "int8_mma_tops": i8.value, "workload": "fwd_d6_n4_b36864",
                           "element_mode_products": elements, "native_fp64_ms": native_ms,
                           "double_float_ms": df_ms, "ozaki": rows}), flush=True)
+        cnt = (ctypes.c_ulonglong * 3)()
+        _lib.check(lib.kronmult_diag_fp64_mma_rounding(cnt), "kronmult_diag_fp64_mma_rounding")
+        share = (ctypes.c_double * 3)()
+        _lib.check(lib.kronmult_diag_fp64_pipe_share(share), "kronmult_diag_fp64_pipe_share")
+        print(json.dumps({"suite": "fp64_tensor_semantics", "elements": cnt[2], "equal_ascending_fma_chain": cnt[0],
+                          "equal_descending_fma_chain": cnt[1], "ms_all_dfma": share[0], "ms_all_dmma": share[1],
+                          "ms_half_each": share[2], "ms_half_each_if_shared": (share[0] + share[1]) / 2,
+                          "ms_half_each_if_separate": max(share[0], share[1]) / 2}), flush=True)
         # the forward on the FP64 tensor path (mma m8n8k4) against the FMA-pipe kernels,
         # same batches (bitwise the same outputs with one output per entry)
         for d, n, n_out, fan in ((2, 8, 14000, 8), (4, 8, 512, 8), (3, 7, 3000, 8), (2, 16, 2000, 8),

@@ -288,6 +288,16 @@ int kronmult_diag_fp64_mma_gflops(double *gflops);
 int kronmult_diag_int8_mma_tops(double *tops);
 int kronmult_diag_ozaki_elementwise_ms(long long elements, int slices, double *ms);
 
+/* Diagnostics of the FP64 tensor path (no reference counterpart; allocate and
+ * synchronise).  kronmult_diag_fp64_mma_rounding: 524,288 elements of m8n8k4 .f64 MMAs
+ * on operands of mixed magnitude (half with C = 0); counts[0] = elements equal to the
+ * k-ascending FMA chain from C, counts[1] = equal to the descending chain, counts[2] =
+ * elements.  kronmult_diag_fp64_pipe_share: ms[0] = all warps on DFMA chains, ms[1] = all
+ * warps on m8n8k4 chains (the same FMA count per warp), ms[2] = half the warps each;
+ * ms[2] near ms[0]/2 + ms[1]/2 means the two share one pipe. */
+int kronmult_diag_fp64_mma_rounding(unsigned long long *counts);
+int kronmult_diag_fp64_pipe_share(double *ms);
+
 /*
  * FP64-accurate forward in emulated arithmetic (no reference counterpart): FP64
  * factors, inputs and outputs; every mode product in double-float (pairs of FP32,

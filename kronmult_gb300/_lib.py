@@ -102,6 +102,8 @@ SIGNATURES = {
     "kronmult_diag_fp64_mma_gflops": (_i, [ctypes.POINTER(ctypes.c_double)]),
     "kronmult_diag_int8_mma_tops": (_i, [ctypes.POINTER(ctypes.c_double)]),
     "kronmult_diag_ozaki_elementwise_ms": (_i, [ctypes.c_longlong, _i, ctypes.POINTER(ctypes.c_double)]),
+    "kronmult_diag_fp64_mma_rounding": (_i, [ctypes.POINTER(ctypes.c_ulonglong)]),
+    "kronmult_diag_fp64_pipe_share": (_i, [ctypes.POINTER(ctypes.c_double)]),
     "kronmult_pow_int": (ctypes.c_longlong, [_i, _i]),
     "kronmult_error_string": (ctypes.c_char_p, [_i]),
     "kronmult_abi_version": (_i, []),

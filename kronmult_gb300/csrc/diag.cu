@@ -177,6 +177,92 @@ int sm_count(int *sms)
     return cudaDeviceGetAttribute(sms, cudaDevAttrMultiProcessorCount, dev);
 }
 
+// ---- how the FP64 tensor path rounds, and whether it shares the FMA pipe ----------
+
+// pseudo-random double of mixed magnitude (exponents 2^-20 .. 2^19) from a 64-bit key
+__device__ __forceinline__ double diag_value(unsigned long long key)
+{
+    unsigned long long z = key * 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    const double u = (double)(z >> 11) * 0x1p-53 * 2.0 - 1.0;  // [-1, 1)
+    return ldexp(u, (int)((z >> 3) % 40) - 20);
+}
+
+// Every warp draws A (8x4), B (4x8) and C (8x8, zero for even tiles), runs one
+// mma.sync.m8n8k4.f64 and compares each of its lane's two outputs with the ascending
+// FMA chain fma(a3,b3, fma(a2,b2, fma(a1,b1, fma(a0,b0,c)))) and with the descending one.
+__global__ void dmma_chain_kernel(unsigned long long *counts, int tiles_per_warp)
+{
+    const int lane = threadIdx.x & 31, g = lane >> 2, s = lane & 3;
+    const unsigned long long warp = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) >> 5;
+    unsigned long long asc = 0, desc = 0, total = 0;
+    for (int t = 0; t < tiles_per_warp; ++t) {
+        const unsigned long long base = (warp * tiles_per_warp + t) * 256ull;
+        auto A = [&](int r, int k) { return diag_value(base + r * 4 + k); };
+        auto B = [&](int k, int c) { return diag_value(base + 64 + k * 8 + c); };
+        auto C = [&](int r, int c) { return (t & 1) ? diag_value(base + 128 + r * 8 + c) : 0.0; };
+        double d0 = C(g, 2 * s), d1 = C(g, 2 * s + 1);
+        const double a = A(g, s), b = B(s, g);
+        asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
+                     : "+d"(d0), "+d"(d1)
+                     : "d"(a), "d"(b));
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const int c = 2 * s + j;
+            double up = C(g, c), down = C(g, c);
+            for (int k = 0; k < 4; ++k) up = fma(A(g, k), B(k, c), up);
+            for (int k = 3; k >= 0; --k) down = fma(A(g, k), B(k, c), down);
+            const double got = j ? d1 : d0;
+            asc += got == up;
+            desc += got == down;
+            ++total;
+        }
+    }
+    atomicAdd(counts + 0, asc);
+    atomicAdd(counts + 1, desc);
+    atomicAdd(counts + 2, total);
+}
+
+// mode 0: every warp runs DFMA chains; 1: every warp runs m8n8k4 chains; 2: even warps
+// DFMA, odd warps DMMA.  Per warp and iteration both do 8 x 256 FMAs.
+__global__ void fp64_mix_kernel(double *out, int iters, int mode)
+{
+    const int w = threadIdx.x >> 5;
+    const bool mma = mode == 1 || (mode == 2 && (w & 1));
+    double s = 0;
+    if (mma) {
+        const double a = 1.0 + 1e-9 * threadIdx.x, b = 1.0 - 1e-9 * threadIdx.x;
+        double c[8][2];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) c[j][0] = c[j][1] = j;
+        for (int i = 0; i < iters; ++i) {
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};"
+                             : "+d"(c[j][0]), "+d"(c[j][1])
+                             : "d"(a), "d"(b));
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) s += c[j][0] + c[j][1];
+    } else {
+        const double a = 1.0 + 1e-9 * threadIdx.x, b = 1e-9;
+        double x[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) x[j] = threadIdx.x + j;
+        for (int i = 0; i < iters; ++i) {
+#pragma unroll
+            for (int r = 0; r < 8; ++r)  // 8 chains x 8 FMAs per lane = 8 x 256 per warp
+#pragma unroll
+                for (int j = 0; j < 8; ++j) x[j] = fma(x[j], a, b);
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) s += x[j];
+    }
+    if (s == 1234.5678) out[0] = s;  // keeps the chains live; never true for these inputs
+}
+
 }  // namespace
 
 extern "C" int kronmult_diag_fp64_mma_gflops(double *gflops)
@@ -259,3 +345,36 @@ extern "C" int kronmult_diag_ozaki_elementwise_ms(long long elements, int slices
     *ms = best;
     return cudaSuccess;
 }
+
+extern "C" int kronmult_diag_fp64_mma_rounding(unsigned long long *counts)
+{
+    if (!counts) return cudaErrorInvalidValue;
+    unsigned long long *d = nullptr;
+    cudaError_t rc = cudaMalloc(&d, 3 * sizeof(unsigned long long));
+    if (rc != cudaSuccess) return rc;
+    cudaMemset(d, 0, 3 * sizeof(unsigned long long));
+    dmma_chain_kernel<<<64, 256>>>(d, 16);  // 512 warps x 16 tiles x 64 elements
+    rc = cudaGetLastError();
+    if (rc == cudaSuccess) rc = cudaMemcpy(counts, d, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return rc;
+}
+
+extern "C" int kronmult_diag_fp64_pipe_share(double *ms)
+{
+    if (!ms) return cudaErrorInvalidValue;
+    int sms = 0;
+    cudaError_t rc = (cudaError_t)sm_count(&sms);
+    if (rc != cudaSuccess) return rc;
+    double *out = nullptr;
+    if ((rc = cudaMalloc(&out, sizeof(double))) != cudaSuccess) return rc;
+    {
+        DiagTimer t;
+        for (int mode = 0; mode < 3; ++mode)
+            ms[mode] = t.best_ms([&] { fp64_mix_kernel<<<sms * 2, 256, 0, t.st>>>(out, 200, mode); }, 3);
+    }
+    rc = cudaGetLastError();
+    cudaFree(out);
+    return rc;
+}
+

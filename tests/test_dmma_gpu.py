@@ -91,3 +91,17 @@ def test_tensor_path_nonfinite_inputs(cuda):
     fin = np.isfinite(want)
     assert np.array_equal(got[fin], want[fin])
     assert np.array_equal(np.isinf(got), np.isinf(want))
+
+
+def test_mma_rounds_as_the_ascending_fma_chain(cuda):
+    """The fact the tensor path rests on: every element of an m8n8k4 .f64 MMA equals the
+    k-ascending FMA chain from C (operands of mixed magnitude), and not a different order."""
+    import ctypes
+
+    from kronmult_gb300 import _lib
+
+    cnt = (ctypes.c_ulonglong * 3)()
+    assert _lib.lib().kronmult_diag_fp64_mma_rounding(cnt) == 0
+    assert cnt[2] == 524288
+    assert cnt[0] == cnt[2]
+    assert cnt[1] < cnt[2] * 0.9
