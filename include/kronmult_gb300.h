@@ -249,11 +249,11 @@ int kronmult_tuning_cache_load(const char *path);
  * Limits: nb_batch <= KRONMULT_NOALLOC_MAX_ENTRIES (else cudaErrorInvalidValue);
  * 2 <= matrix_size <= 8, n^(d-1) <= 1024 (at most 4 fibres per thread of a
  * 256-thread team) and n^d fitting one team's shared memory (else
- * cudaErrorNotSupported; e.g. n = 2, d = 12 is refused).  The first call on a
- * device looks up the array's device address (cudaGetSymbolAddress) with that
- * device current, under a lock, and keeps it for the process: make that first call
- * before any stream capture, and do not call this entry point on a device after
- * cudaDeviceReset.  All calls share the array and it keeps the last call's contents
+ * cudaErrorNotSupported; e.g. n = 2, d = 12 is refused).  Every call looks up the
+ * array's device address in the current context (cudaGetSymbolAddress: no
+ * allocation, no cached state, so a context re-created after cudaDeviceReset is
+ * served correctly); make the first call on a device before any stream capture (it
+ * may load the module).  All calls share the array and it keeps the last call's contents
  * (its counters are cleared at the start of every call): calls that overlap on the
  * GPU (other streams, other host threads) race and must be serialised.
  */

@@ -28,7 +28,6 @@
 // Calls that overlap on the GPU (concurrent streams, or several host threads)
 // race on the array and must be serialised by the caller.
 #include <climits>
-#include <mutex>
 #include "fwd_kernels.cuh"
 #include "kronmult_gb300.h"
 
@@ -114,30 +113,21 @@ NaFn noalloc_lookup(int nn, int qmax)
 #undef KGB_NA
 }
 
-// Device address of the scratch array, looked up once per device with that device
-// current (host code cannot use the array's name as a device address).  Fixed-size
-// table, filled under a lock so that concurrent first calls from several host threads
-// are safe.  No allocation.  The address belongs to the device's current context: after
-// cudaDeviceReset the cached value would be stale, so a process that resets a device
-// must not call this entry point on it again.
-constexpr int kMaxDevices = 64;
-void *g_scratch_ptr[kMaxDevices] = {};
-std::mutex g_scratch_mutex;
-
+// Device address of the scratch array in the current device's context, looked up on
+// every call (host code cannot use the array's name as a device address).  The lookup
+// allocates nothing and keeps no state, so concurrent calls from several host threads
+// need no lock and a context re-created after cudaDeviceReset is never served a stale
+// address.
 int scratch_address(int dev, void **out)
 {
-    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (g_scratch_ptr[dev] == nullptr) {
-        void *p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) {
-            cudaGetLastError();  // leave no sticky status behind for later, unrelated calls
-            return e;
-        }
-        g_scratch_ptr[dev] = p;
+    (void)dev;
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) {
+        cudaGetLastError();  // leave no sticky status behind for later, unrelated calls
+        return e;
     }
-    *out = g_scratch_ptr[dev];
+    *out = p;
     return cudaSuccess;
 }
 
