@@ -105,3 +105,26 @@ def test_mma_rounds_as_the_ascending_fma_chain(cuda):
     assert cnt[2] == 524288
     assert cnt[0] == cnt[2]
     assert cnt[1] < cnt[2] * 0.9
+
+
+@pytest.mark.parametrize("d,n", [(6, 3), (4, 4), (3, 6), (2, 8)])
+def test_fp64_mappings_same_bits(cuda, d, n):
+    """kronmult_tuning.fp64_path 3 (whole fibres per thread) and 4 (one output element per
+    thread) on the FMA pipe, single call and grouped plan: the same k-ascending chains, so
+    with one output per entry every choice gives the same bits."""
+    from kronmult_gb300 import DeviceBatch
+    from kronmult_gb300 import workloads as W
+    from kronmult_gb300.grouped import GroupedPlan
+
+    b = W.make_batch(d, n, n, 50, 1, seed=7700 + 10 * d + n)
+    outs = [_run(b, cuda, t) for t in (None, {"fp64_path": 3}, {"fp64_path": 4})]
+    for t in ({"fp64_path": 3}, {"fp64_path": 4}):
+        db = DeviceBatch.from_host(b, device=cuda)
+        plan = GroupedPlan([db], mode="atomic", tunings=[t])
+        plan.run()
+        torch.cuda.synchronize()
+        outs.append(db.outputs.clone())
+        plan.close()
+    for o in outs[1:]:
+        assert torch.equal(o, outs[0])
+    assert O.rel_l2(outs[0].cpu().numpy(), O.forward(b)) <= TOL64
