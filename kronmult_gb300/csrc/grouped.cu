@@ -399,7 +399,7 @@ int grouped_plan_create(GroupedPlan *&out, const kronmult_group *groups, int n_g
         if (tunings && tunings[g].entries_per_team > 0) unit = tunings[g].entries_per_team;
         a.unit = std::max(1LL, unit);
         a.n_units = (a.nb + a.unit - 1) / a.unit;
-        if (a.n_units > (long long)UINT_MAX) {
+        if (a.n_units > (long long)UINT_MAX - (1LL << 24)) {  // room for every team's claim ahead
             rc = cudaErrorInvalidValue;
             break;
         }

@@ -29,7 +29,8 @@ __global__ void __launch_bounds__(kGroupedBlock, 3) gq_df_kernel(const GqArgs a)
     const double *const *in = reinterpret_cast<const double *const *>(a.in);
     double *const *out = reinterpret_cast<double *const *>(a.out);
     long long b, e;
-    while (gq_next(a, &s_unit[tm.id], tm, b, e)) {
+    unsigned claim = gq_first_claim(a, tm);
+    while (gq_next(a, &s_unit[tm.id], tm, claim, b, e)) {
         long long rs = b;
         for (long long ei = b; ei < e; ++ei) {
             bool first, last;

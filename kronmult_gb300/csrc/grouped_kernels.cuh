@@ -14,10 +14,24 @@
 
 namespace kgb {
 
-// the team's next unit as [b, e) of the group's order; false when the queue is empty
-__device__ __forceinline__ bool gq_next(const GqArgs &a, long long *slot, const Team &tm, long long &b, long long &e)
+// A team's claims on the queue run one unit ahead: rank 0 claims the next unit while the
+// team computes the current one, so the atomic's round trip to L2 overlaps work instead
+// of stalling the team once per unit (units are single entries in the FP64 atomic mode).
+// A team holding a claim beyond the queue's end stops; the counter may pass n_units by
+// at most one claim per team (it is reset before every run).
+__device__ __forceinline__ unsigned gq_first_claim(const GqArgs &a, const Team &tm)
 {
-    if (tm.rank == 0) *slot = (long long)atomicAdd(a.queue, 1u);
+    return tm.rank == 0 ? atomicAdd(a.queue, 1u) : 0u;
+}
+
+// the team's next unit as [b, e) of the group's order; false when the queue is empty
+__device__ __forceinline__ bool gq_next(const GqArgs &a, long long *slot, const Team &tm, unsigned &claim,
+                                        long long &b, long long &e)
+{
+    if (tm.rank == 0) {
+        *slot = (long long)claim;
+        if ((long long)claim < a.n_units) claim = atomicAdd(a.queue, 1u);  // the unit after this one
+    }
     tm.sync();
     const long long u = *slot;
     tm.sync();
@@ -180,7 +194,8 @@ __global__ void __launch_bounds__(kGroupedBlock, sizeof(T) == 8 ? 3 : 4) gq_fibr
     const T *const *in = reinterpret_cast<const T *const *>(a.in);
     TO *const *out = reinterpret_cast<TO *const *>(a.out);
     long long b, e;
-    while (gq_next(a, &s_unit[tm.id], tm, b, e))
+    unsigned claim = gq_first_claim(a, tm);
+    while (gq_next(a, &s_unit[tm.id], tm, claim, b, e))
     {
         long long rs = b;
         for (long long ei = b; ei < e; ++ei) {
@@ -210,7 +225,8 @@ __global__ void __launch_bounds__(kGroupedBlock, sizeof(T) == 8 ? (DET || EMAX >
     const T *const *in = reinterpret_cast<const T *const *>(a.in);
     TO *const *out = reinterpret_cast<TO *const *>(a.out);
     long long b, e;
-    while (gq_next(a, &s_unit[tm.id], tm, b, e))
+    unsigned claim = gq_first_claim(a, tm);
+    while (gq_next(a, &s_unit[tm.id], tm, claim, b, e))
     {
         long long rs = b;
         for (long long ei = b; ei < e; ++ei) {
@@ -235,7 +251,8 @@ __global__ void __launch_bounds__(kGroupedBlock, 2) gq_elem_rt_kernel(const GqAr
     const T *const *in = reinterpret_cast<const T *const *>(a.in);
     TO *const *out = reinterpret_cast<TO *const *>(a.out);
     long long b, e;
-    while (gq_next(a, &s_unit[tm.id], tm, b, e))
+    unsigned claim = gq_first_claim(a, tm);
+    while (gq_next(a, &s_unit[tm.id], tm, claim, b, e))
         team_forward_elem<T, TO, EMAX, DET>(mats, in, out, nullptr, a.d, a.n, a.stride, a.N, b, e, buf, fac, tm);
 }
 
