@@ -122,8 +122,11 @@ __device__ __forceinline__ void mode_slow_elem(T *buf, const T *M, int n_rt, int
     tm.sync();
 }
 
-template <typename T, int NN, int EMAX>
-__global__ void __launch_bounds__(512) adj_elem_kernel(const AdjArgs<T> a)
+// OCC: the FP64 form for teams of at most 256 threads with at most 4 outputs per thread,
+// bounded to 80 registers (no spills) so that 3 CTAs of 256 threads fit an SM; the
+// default form admits teams of up to 512 threads.
+template <typename T, int NN, int EMAX, bool OCC = false>
+__global__ void __launch_bounds__(OCC ? 256 : 512, OCC ? 3 : 1) adj_elem_kernel(const AdjArgs<T> a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const Team tm(a.team_size);
@@ -431,6 +434,8 @@ __global__ void __launch_bounds__(256, 3) adj_smem_kernel(const AdjArgs<T> a)
 
 template <typename T> using AdjFn = void (*)(const AdjArgs<T>);
 template <typename T> AdjFn<T> adj_lookup(int nn, int emax);
+// the 3-CTA form (OCC) for compile-time n = 2..8 and EMAX <= 4; null otherwise
+template <typename T> AdjFn<T> adj_occ_lookup(int nn, int emax);
 template <typename T> AdjFn<T> adj_fibre_lookup(int nn, int qmax);
 
 }  // namespace kgb
@@ -443,6 +448,11 @@ template <typename T> AdjFn<T> adj_fibre_lookup(int nn, int qmax);
     case NN * 32 + 8: return adj_elem_kernel<T, NN, 8>;                                                \
     case NN * 32 + 16: return adj_elem_kernel<T, NN, 16>;
 
+#define KGB_ADJ_OCC_CASES(T, NN)                                                                       \
+    case NN * 32 + 1: return adj_elem_kernel<T, NN, 1, true>;                                          \
+    case NN * 32 + 2: return adj_elem_kernel<T, NN, 2, true>;                                          \
+    case NN * 32 + 4: return adj_elem_kernel<T, NN, 4, true>;
+
 // run-time n only (nn is ignored)
 #define KGB_ADJ_INSTANTIATE(T)                                                                         \
     namespace kgb {                                                                                    \
@@ -453,6 +463,7 @@ template <typename T> AdjFn<T> adj_fibre_lookup(int nn, int qmax);
         default: return nullptr;                                                                       \
         }                                                                                              \
     }                                                                                                  \
+    template <> AdjFn<T> adj_occ_lookup<T>(int, int) { return nullptr; }                               \
     }
 
 // compile-time n for 2 <= n <= 8, run-time n otherwise
@@ -469,6 +480,19 @@ template <typename T> AdjFn<T> adj_fibre_lookup(int nn, int qmax);
             KGB_ADJ_ELEM_CASES(T, 6)                                                                   \
             KGB_ADJ_ELEM_CASES(T, 7)                                                                   \
             KGB_ADJ_ELEM_CASES(T, 8)                                                                   \
+        default: return nullptr;                                                                       \
+        }                                                                                              \
+    }                                                                                                  \
+    template <> AdjFn<T> adj_occ_lookup<T>(int nn, int emax)                                           \
+    {                                                                                                  \
+        switch (nn * 32 + emax) {                                                                      \
+            KGB_ADJ_OCC_CASES(T, 2)                                                                    \
+            KGB_ADJ_OCC_CASES(T, 3)                                                                    \
+            KGB_ADJ_OCC_CASES(T, 4)                                                                    \
+            KGB_ADJ_OCC_CASES(T, 5)                                                                    \
+            KGB_ADJ_OCC_CASES(T, 6)                                                                    \
+            KGB_ADJ_OCC_CASES(T, 7)                                                                    \
+            KGB_ADJ_OCC_CASES(T, 8)                                                                    \
         default: return nullptr;                                                                       \
         }                                                                                              \
     }                                                                                                  \

@@ -128,11 +128,28 @@ static int adjoint_async(int d, int n, const T *const *mats, int stride, const T
             return cudaErrorInvalidValue;
         ts = elem_team_size(N, 16, tune && tune->team_size > 0 ? tune->team_size : 0, 512);
         if (ts == 0) return cudaErrorNotSupported;
-        const int per = (N + ts - 1) / ts;
+        int per = (N + ts - 1) / ts;
         int emax = 1;
         while (emax < per) emax *= 2;
         if (emax > 16) return cudaErrorNotSupported;
         fn = adj_lookup<T>(n, emax);
+        // FP64, compile-time n: the smallest team of at least a warp that leaves each thread
+        // at most 4 outputs with the same lane use (counted in issued warp rounds) runs the
+        // 80-register form at 3 CTAs of 256 threads per SM instead of 2
+        if (sizeof(T) == 8 && !(tune && tune->team_size > 0)) {
+            int t4 = 32;
+            while (t4 < 256 && (N + t4 - 1) / t4 > 4) t4 *= 2;
+            const int per4 = (N + t4 - 1) / t4;
+            int emax4 = 1;
+            while (emax4 < per4) emax4 *= 2;
+            const AdjFn<T> f4 = per4 <= 4 ? adj_occ_lookup<T>(n, emax4) : nullptr;
+            if (f4 && lane_use(N, t4) >= lane_use(N, ts) - 0.02) {
+                fn = f4;
+                ts = t4;
+                per = per4;
+                emax = emax4;
+            }
+        }
         if (!fn) return cudaErrorNotSupported;
         // gradient contraction items (pair, slice of t): S slices cost about
         // ceil(S*P / lanes) passes of ceil(R / S) FMAs plus ceil(P / lanes) passes of S
