@@ -179,7 +179,7 @@ typedef struct kronmult_grouped_plan_s *kronmult_grouped_plan;
 int kronmult_grouped_plan_create(kronmult_grouped_plan *plan, const kronmult_group *groups, int n_groups, int dtype,
                                  int mode, const kronmult_tuning *tunings);
 int kronmult_grouped_run(kronmult_grouped_plan plan, void *stream);
-/* info[0..5] = largest grid, block, largest dynamic shared bytes, work units (all
+/* info[0..5] = largest grid, largest block (threads per CTA, at most 256), largest dynamic shared bytes, work units (all
  * groups), kernels per run (forward groups + adjoint groups), entries ordered on the
  * device (deterministic mode) */
 int kronmult_grouped_plan_info(kronmult_grouped_plan plan, long long *info, int n_info);

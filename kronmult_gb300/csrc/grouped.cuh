@@ -43,6 +43,9 @@ using GqFn = void (*)(const GqArgs);
 // mapping with n at run time (n = 9..16).  Null when no instantiation fits.
 template <typename T, typename TO> GqFn gq_fibre_lookup(int nn, int qmax, bool det);
 template <typename T, typename TO> GqFn gq_elem_lookup(int nn, int emax, bool det);
+// the element mapping with each thread's factor row in registers (team size a multiple
+// of n and of 32; EMAX 2 or 4; n = 4, 8)
+template <typename T, typename TO> GqFn gq_elem_rows_lookup(int nn, int emax, bool det);
 template <typename T, typename TO> GqFn gq_elem_rt_lookup(int emax, bool det);
 
 // Double-float kernel for a group (FP64 data, FP32-pipe arithmetic; n = 2..8, QMAX
@@ -61,7 +64,7 @@ void gq_group_launch(const void *const *mats, const void *const *in, const void 
 
 struct GqLaunch {
     GqFn fn = nullptr;
-    int grid = 0;
+    int grid = 0, block = kGroupedBlock;
     size_t smem = 0;
     GqArgs args{};
     // deterministic mode: sort buffers (m = power of two >= nb entries) and the group's

@@ -111,13 +111,17 @@ __device__ __forceinline__ void gq_entry_fibre(const T *const *mats, const T *co
 // goes to the other buffer as soon as it is computed (the last mode's straight into the
 // output), so a mode ends with one barrier and no results wait in registers.  The
 // barrier before staging keeps the previous entry's last reads ahead of the new copy.
-template <typename T, typename TO, int NN, int EMAX, bool DET>
+// ROWS (team size a multiple of n): every element a thread owns has the same row
+// r = rank mod n, so the thread reads that row of each factor into registers once per
+// mode instead of once per element.
+template <typename T, typename TO, int NN, int EMAX, bool DET, bool ROWS = false>
 __device__ __forceinline__ void gq_entry_elem(const T *const *mats, const T *const *in, TO *const *out, int d,
                                               int stride, int N, long long e, T *buf, T *buf2, T *fac, T *acc,
                                               T *part, bool first, bool last, const Team &tm)
 {
     constexpr int P = NN * NN;
     const int F = N / NN;
+    const int r0 = tm.rank % NN;
     tm.sync();
     stage_vector(buf, in[e], N, tm);
     stage_factors<T, NN>(fac, mats + e * d, d, stride, tm);
@@ -127,16 +131,21 @@ __device__ __forceinline__ void gq_entry_elem(const T *const *mats, const T *con
     T *dst = buf2;
     for (int i = d - 1; i >= 0; --i) {
         const T *M = fac + i * P;
+        T mrow[NN];
+        if constexpr (ROWS) {
+#pragma unroll
+            for (int k = 0; k < NN; ++k) mrow[k] = M[r0 + k * NN];
+        }
 #pragma unroll
         for (int j = 0; j < EMAX; ++j) {
             const int q = tm.rank + j * tm.size;
             if (q < N) {
-                const int c = q / NN, r = q - c * NN;
+                const int c = q / NN, r = ROWS ? r0 : q - c * NN;
                 T x[NN];
                 load_fibre<T, NN>(src + c * NN, x);
                 T s = T(0);
 #pragma unroll
-                for (int k = 0; k < NN; ++k) s = fma_t<T>(M[r + k * NN], x[k], s);
+                for (int k = 0; k < NN; ++k) s = fma_t<T>(ROWS ? mrow[k] : M[r + k * NN], x[k], s);
                 if (i > 0)
                     dst[c + r * F] = s;
                 else
@@ -208,9 +217,10 @@ __global__ void __launch_bounds__(kGroupedBlock, sizeof(T) == 8 ? 3 : 4) gq_fibr
 }
 
 // FP64 atomic mode with at most 4 outputs per thread fits 48 registers without spills:
-// 5 CTAs of 256 threads per SM (more warps to keep the FP64 pipe fed across barriers).
-template <typename T, typename TO, int NN, int EMAX, bool DET>
-__global__ void __launch_bounds__(kGroupedBlock, sizeof(T) == 8 ? (DET || EMAX > 4 ? 3 : 5) : 4)
+// 5 CTAs of 256 threads per SM (more warps to keep the FP64 pipe fed across barriers);
+// the rows form holds n more values and gets 64 registers (4 CTAs).
+template <typename T, typename TO, int NN, int EMAX, bool DET, bool ROWS = false>
+__global__ void __launch_bounds__(kGroupedBlock, sizeof(T) == 8 ? (DET || EMAX > 4 ? 3 : (ROWS ? 4 : 5)) : 4)
     gq_elem_kernel(const GqArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -232,8 +242,8 @@ __global__ void __launch_bounds__(kGroupedBlock, sizeof(T) == 8 ? (DET || EMAX >
         for (long long ei = b; ei < e; ++ei) {
             bool first, last;
             T *part = gq_run_edges<T, DET>(a, b, e, ei, rs, first, last);
-            gq_entry_elem<T, TO, NN, EMAX, DET>(mats, in, out, a.d, a.stride, a.N, ei, buf, buf2, fac, acc, part,
-                                                first, last, tm);
+            gq_entry_elem<T, TO, NN, EMAX, DET, ROWS>(mats, in, out, a.d, a.stride, a.N, ei, buf, buf2, fac, acc,
+                                                      part, first, last, tm);
         }
     }
 }
@@ -271,6 +281,10 @@ __global__ void __launch_bounds__(kGroupedBlock, 2) gq_elem_rt_kernel(const GqAr
     case NN * 32 + E * 2: return gq_elem_kernel<KGB_T, KGB_TO, NN, E, false>;                              \
     case NN * 32 + E * 2 + 1: return gq_elem_kernel<KGB_T, KGB_TO, NN, E, true>;
 #define KGB_GQ_E(NN) KGB_GQ_E1(NN, 1) KGB_GQ_E1(NN, 2) KGB_GQ_E1(NN, 4) KGB_GQ_E1(NN, 8)
+#define KGB_GQ_ER1(NN, E)                                                                                  \
+    case NN * 32 + E * 2: return gq_elem_kernel<KGB_T, KGB_TO, NN, E, false, true>;                        \
+    case NN * 32 + E * 2 + 1: return gq_elem_kernel<KGB_T, KGB_TO, NN, E, true, true>;
+#define KGB_GQ_ER(NN) KGB_GQ_ER1(NN, 2) KGB_GQ_ER1(NN, 4)
 #define KGB_GQ_R(E)                                                                                        \
     case E * 2: return gq_elem_rt_kernel<KGB_T, KGB_TO, E, false>;                                         \
     case E * 2 + 1: return gq_elem_rt_kernel<KGB_T, KGB_TO, E, true>;
@@ -297,6 +311,14 @@ __global__ void __launch_bounds__(kGroupedBlock, 2) gq_elem_rt_kernel(const GqAr
             KGB_GQ_E(2) KGB_GQ_E(3) KGB_GQ_E(4) KGB_GQ_E(5) KGB_GQ_E(6) KGB_GQ_E(7) KGB_GQ_E(8)             \
         default: return nullptr;                                                                           \
         }                                                                                                  \
+    }                                                                                                      \
+    template <> GqFn gq_elem_rows_lookup<KGB_T, KGB_TO>(int nn, int emax, bool det)                        \
+    {                                                                                                      \
+        switch (nn * 32 + emax * 2 + (det ? 1 : 0)) {                                                      \
+            KGB_GQ_ER(4) KGB_GQ_ER(8)                                                                      \
+        default: return nullptr;                                                                           \
+        }                                                                                                  \
     }
 #define KGB_GQ_LOOKUP_NO_ELEM                                                                              \
-    template <> GqFn gq_elem_lookup<KGB_T, KGB_TO>(int, int, bool) { return nullptr; }
+    template <> GqFn gq_elem_lookup<KGB_T, KGB_TO>(int, int, bool) { return nullptr; }                     \
+    template <> GqFn gq_elem_rows_lookup<KGB_T, KGB_TO>(int, int, bool) { return nullptr; }

@@ -38,7 +38,7 @@ def test_config3_groups(cuda, mode):
     for b, db in zip(batches, dbs):
         assert O.rel_l2(db.outputs.cpu().numpy(), O.forward(b)) <= TOL64
     info = plan.info()
-    assert info["items"] > 0 and info["grid"] > 0 and info["block"] == 256
+    assert info["items"] > 0 and info["grid"] > 0 and 32 <= info["block"] <= 256 and info["block"] % 32 == 0
 
 
 def test_deterministic_is_bitwise_reproducible(cuda):
