@@ -118,9 +118,8 @@ NaFn noalloc_lookup(int nn, int qmax)
 // allocates nothing and keeps no state, so concurrent calls from several host threads
 // need no lock and a context re-created after cudaDeviceReset is never served a stale
 // address.
-int scratch_address(int dev, void **out)
+int scratch_address(void **out)
 {
-    (void)dev;
     void *p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) {
@@ -156,7 +155,7 @@ extern "C" int kronmult_batched_f64_noalloc(int matrix_count, int matrix_size,
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     void *scratch = nullptr;
-    int rc = scratch_address(dev, &scratch);
+    int rc = scratch_address(&scratch);
     if (rc != cudaSuccess) return rc;
     int sms = 0, smem_optin = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
