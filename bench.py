@@ -596,7 +596,8 @@ def suite(args):
 
     # C4: FP32 storage, FP32 / TF32 / BF16 contraction, FP64 outputs
     modes4 = [(c, k) for c, k in (("fp32", _lib.KRONMULT_COMPUTE_FP32), ("tf32", _lib.KRONMULT_COMPUTE_TF32),
-                                  ("bf16", _lib.KRONMULT_COMPUTE_BF16)) if want(f"c4_fwd_{c}")]
+                                  ("bf16", _lib.KRONMULT_COMPUTE_BF16), ("bf16x3", _lib.KRONMULT_COMPUTE_BF16X3))
+              if want(f"c4_fwd_{c}")]
     b = W.config4(scale=sc) if modes4 else None
     ref = O.forward(b) if modes4 else None
     db = DeviceBatch.from_host(b, device=dev, dtype=torch.float32, out_dtype=torch.float64) if modes4 else None

@@ -42,6 +42,9 @@ extern "C" {
 #define KRONMULT_COMPUTE_FP32 0 /* FP32 FMA on CUDA cores */
 #define KRONMULT_COMPUTE_TF32 1 /* TF32 tensor-core mode products (n == 8), FP32 accumulate */
 #define KRONMULT_COMPUTE_BF16 2 /* BF16 tensor-core mode products (n == 8), FP32 accumulate */
+#define KRONMULT_COMPUTE_BF16X3 3 /* split BF16 (v = hi + lo) tensor-core mode products, three MMAs
+                                     (hi.hi + lo.hi + hi.lo) per product, FP32 accumulate (n == 8):
+                                     about 16 significand bits per product */
 
 /* Storage/output type codes. */
 #define KRONMULT_DTYPE_F64 0        /* double factors, inputs and outputs */

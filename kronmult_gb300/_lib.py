@@ -14,6 +14,7 @@ LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libkronmult
 KRONMULT_COMPUTE_FP32 = 0
 KRONMULT_COMPUTE_TF32 = 1
 KRONMULT_COMPUTE_BF16 = 2
+KRONMULT_COMPUTE_BF16X3 = 3
 
 
 class Tuning(ctypes.Structure):

@@ -289,7 +289,7 @@ int kronmult_batched_f32_f64out_async(int matrix_count, int matrix_size, const f
                                       double *const *output_batched, float *const *workspace_batched,
                                       int nb_batch, int compute, void *stream, const kronmult_tuning *tuning)
 {
-    if (compute == KRONMULT_COMPUTE_TF32 || compute == KRONMULT_COMPUTE_BF16) {
+    if (compute == KRONMULT_COMPUTE_TF32 || compute == KRONMULT_COMPUTE_BF16 || compute == KRONMULT_COMPUTE_BF16X3) {
         if (matrix_count < 0 || matrix_size < 0 || nb_batch < 0 || matrix_stride < (matrix_size > 0 ? matrix_size : 1))
             return cudaErrorInvalidValue;
         if (nb_batch == 0) return cudaSuccess;

@@ -230,6 +230,27 @@ __device__ __forceinline__ float to_tf32(float x)
     return __uint_as_float(r);
 }
 
+// 8 FP32 values split into BF16 pairs v = hi + lo: hi rounded to nearest, lo the rounded
+// remainder (v - hi is exact in FP32), each set packed in order into 16 bytes
+__device__ __forceinline__ void split_bf16x8(const float (&v)[8], uint4 &hi, uint4 &lo)
+{
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const __nv_bfloat162 hb = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+        h[i] = *reinterpret_cast<const uint32_t *>(&hb);
+        // hi back in FP32 (a BF16 value is the upper half of its FP32 bits), both lanes at
+        // once; the remainders with one packed subtraction
+        const f2 hf = ((unsigned long long)(h[i] & 0xFFFF0000u) << 32) | ((unsigned long long)(h[i] & 0xFFFFu) << 16);
+        float r0, r1;
+        f2_unpack(f2_sub(f2_pack(v[2 * i], v[2 * i + 1]), hf), r0, r1);
+        const __nv_bfloat162 lb = __floats2bfloat162_rn(r0, r1);
+        l[i] = *reinterpret_cast<const uint32_t *>(&lb);
+    }
+    hi = make_uint4(h[0], h[1], h[2], h[3]);
+    lo = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
 // store one value of the operand element (row, k) in the operand type of KIND: B
 // operands (factors) in the plain core-matrix layout, A (lbo != 0) in the split one
 template <int KIND>
@@ -505,15 +526,24 @@ template <int KIND> __global__ void __launch_bounds__(kTcThreads, 6) fwd_tc_kern
 // fwd_tc_kernel: one staging slot refilled by a bulk copy while the current entry's
 // modes run, factors one entry ahead in registers, runs of entries with one output
 // summed in TMEM, bounded mbarrier waits.
-__global__ void __launch_bounds__(kTcThreads, 8) fwd_tc_bf16_kernel(const TcArgs a)
+// SPLIT (KRONMULT_COMPUTE_BF16X3): every operand value v is held as two BF16 values,
+// hi = bf16(v) and lo = bf16(v - hi), and each tile pair runs three MMAs into one FP32
+// accumulator, x_hi.A_hi + x_lo.A_hi + x_hi.A_lo (the lo.lo term, 2^-16 relative, is
+// dropped): about 16 significand bits per product instead of 8.  The hi and lo vector
+// operands and factor operands sit side by side in the same layouts.
+template <bool SPLIT>
+__global__ void __launch_bounds__(kTcThreads, SPLIT ? 5 : 8) fwd_tc_bf16_kernel(const TcArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int N = a.N, F = N / 8, d = a.d;
     const int pairs = (a.tiles + 1) / 2;
+    constexpr int kParts = SPLIT ? 2 : 1;
     float *raw = reinterpret_cast<float *>(smem_raw);                          // staging slot, N floats
-    unsigned char *xs = reinterpret_cast<unsigned char *>(raw + N);           // pairs x kPairBytes
-    unsigned char *bs = xs + (size_t)pairs * kPairBytes + 64;                 // d x [A_i 0; 0 A_i]
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(bs + (size_t)d * kBf16B);  // MMA completion
+    unsigned char *xs = reinterpret_cast<unsigned char *>(raw + N);           // pairs x kPairBytes (hi)
+    unsigned char *xl = xs + (size_t)pairs * kPairBytes;                      // the lo parts (SPLIT)
+    unsigned char *bs = xs + (size_t)kParts * pairs * kPairBytes + 64;        // d x [A_i 0; 0 A_i] (hi)
+    unsigned char *bl = bs + (size_t)d * kBf16B;                              // the lo parts (SPLIT)
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(bs + (size_t)kParts * d * kBf16B);  // MMA completion
     uint64_t *sbar = mbar + 1;                                                // staging completion
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 2);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -524,7 +554,7 @@ __global__ void __launch_bounds__(kTcThreads, 8) fwd_tc_bf16_kernel(const TcArgs
 
     // operands zeroed once: fibres beyond F, the odd K half of an unpaired tile and the
     // off-diagonal blocks of the factor operands stay zero
-    for (int v = tid; v < (int)(pairs * kPairBytes + 64 + d * kBf16B) / 16; v += kTcThreads)
+    for (int v = tid; v < (int)(kParts * pairs * kPairBytes + 64 + kParts * d * kBf16B) / 16; v += kTcThreads)
         reinterpret_cast<int4 *>(xs)[v] = make_int4(0, 0, 0, 0);
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
@@ -550,7 +580,7 @@ __global__ void __launch_bounds__(kTcThreads, 8) fwd_tc_bf16_kernel(const TcArgs
     const uint32_t tacc = tmem + 16u * pairs;  // run accumulator after the mode output
     const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
     const uint32_t mbar_a = smem_u32(mbar);
-    const uint32_t xs_a = smem_u32(xs), bs_a = smem_u32(bs);
+    const uint32_t xs_a = smem_u32(xs), bs_a = smem_u32(bs), xl_a = smem_u32(xl), bl_a = smem_u32(bl);
     uint32_t phase = 0, sphase = 0;
     bool failed = false;
     bool staging = true;  // a staging copy is in flight whose phase has not been waited for
@@ -614,12 +644,23 @@ __global__ void __launch_bounds__(kTcThreads, 8) fwd_tc_bf16_kernel(const TcArgs
                 const int i = v >> 6, r = v & 7, k = (v >> 3) & 7;
                 put<KIND_BF16>(bs + (size_t)i * kBf16B, r, k, fv[s]);
                 put<KIND_BF16>(bs + (size_t)i * kBf16B, r + 8, k + 8, fv[s]);
+                if constexpr (SPLIT) {
+                    const float rem = fv[s] - __bfloat162float(__float2bfloat16_rn(fv[s]));
+                    put<KIND_BF16>(bl + (size_t)i * kBf16B, r, k, rem);
+                    put<KIND_BF16>(bl + (size_t)i * kBf16B, r + 8, k + 8, rem);
+                }
             }
         }
         // vector operand: natural position p = fibre + F*K (K = the slowest index, mode 0,
         // contracted first), so 8 consecutive positions are 8 consecutive fibres of one K row
         if (d == 1) {
-            if (tid < 8) *reinterpret_cast<__nv_bfloat16 *>(xs + tid * 16) = __float2bfloat16_rn(raw[tid]);
+            if (tid < 8) {
+                const __nv_bfloat16 h = __float2bfloat16_rn(raw[tid]);
+                *reinterpret_cast<__nv_bfloat16 *>(xs + tid * 16) = h;
+                if constexpr (SPLIT)
+                    *reinterpret_cast<__nv_bfloat16 *>(xl + tid * 16) =
+                        __float2bfloat16_rn(raw[tid] - __bfloat162float(h));
+            }
         } else {
             const uint32_t fsh = 3u * (uint32_t)(d - 1);
             for (int q = tid; q < N / 8; q += kTcThreads) {
@@ -630,8 +671,16 @@ __global__ void __launch_bounds__(kTcThreads, 8) fwd_tc_bf16_kernel(const TcArgs
                 const float4 second = *reinterpret_cast<const float4 *>(raw + 8 * q + 4 * (h ^ 1));
                 const float4 u = h ? second : first, w = h ? first : second;
                 const uint32_t p0 = 8u * (uint32_t)q;
-                *reinterpret_cast<uint4 *>(xs + mn_offset((p0 & (uint32_t)(F - 1)) >> 3, p0 >> fsh)) =
-                    pack_bf16x8(u.x, u.y, u.z, u.w, w.x, w.y, w.z, w.w);
+                const uint32_t off = mn_offset((p0 & (uint32_t)(F - 1)) >> 3, p0 >> fsh);
+                if constexpr (SPLIT) {
+                    const float v8[8] = {u.x, u.y, u.z, u.w, w.x, w.y, w.z, w.w};
+                    uint4 hi, lo;
+                    split_bf16x8(v8, hi, lo);
+                    *reinterpret_cast<uint4 *>(xs + off) = hi;
+                    *reinterpret_cast<uint4 *>(xl + off) = lo;
+                } else {
+                    *reinterpret_cast<uint4 *>(xs + off) = pack_bf16x8(u.x, u.y, u.z, u.w, w.x, w.y, w.z, w.w);
+                }
             }
         }
         // the run continues when this entry adds into the same output as the previous one;
@@ -654,9 +703,16 @@ __global__ void __launch_bounds__(kTcThreads, 8) fwd_tc_bf16_kernel(const TcArgs
                 tc_fence_after();
                 const uint32_t dst = last ? tacc : tmem;
                 const uint32_t accumulate = (last && cont) ? 1u : 0u;
-                for (int j = 0; j < pairs; ++j)
+                for (int j = 0; j < pairs; ++j) {
                     mma_bf16_mn(dst + 16u * (uint32_t)j, smem_desc(xs_a + j * kPairBytes, kMnLbo, kMnSbo),
                                 smem_desc(bs_a + i * kBf16B), accumulate);
+                    if constexpr (SPLIT) {
+                        mma_bf16_mn(dst + 16u * (uint32_t)j, smem_desc(xl_a + j * kPairBytes, kMnLbo, kMnSbo),
+                                    smem_desc(bs_a + i * kBf16B), 1u);
+                        mma_bf16_mn(dst + 16u * (uint32_t)j, smem_desc(xs_a + j * kPairBytes, kMnLbo, kMnSbo),
+                                    smem_desc(bl_a + i * kBf16B), 1u);
+                    }
+                }
                 mma_commit(mbar_a);
             }
             const bool ok = mbar_wait(mbar_a, phase);
@@ -685,8 +741,15 @@ __global__ void __launch_bounds__(kTcThreads, 8) fwd_tc_bf16_kernel(const TcArgs
                             if (t < a.tiles && c < F) {
                                 const float(&v)[8] = h ? v1 : v0;
                                 const uint32_t kk = (uint32_t)c >> sh, g = (uint32_t)c & ((1u << sh) - 1u);
-                                *reinterpret_cast<uint4 *>(xs + mn_offset(g, kk)) =
-                                    pack_bf16x8(v[0], v[1], v[2], v[3], v[4], v[5], v[6], v[7]);
+                                if constexpr (SPLIT) {
+                                    uint4 hi, lo;
+                                    split_bf16x8(v, hi, lo);
+                                    *reinterpret_cast<uint4 *>(xs + mn_offset(g, kk)) = hi;
+                                    *reinterpret_cast<uint4 *>(xl + mn_offset(g, kk)) = lo;
+                                } else {
+                                    *reinterpret_cast<uint4 *>(xs + mn_offset(g, kk)) =
+                                        pack_bf16x8(v[0], v[1], v[2], v[3], v[4], v[5], v[6], v[7]);
+                                }
                             }
                         }
                     }
@@ -735,9 +798,11 @@ int launch_tc_forward(int kind, int d, int n, const float *const *mats, int stri
     int cols = 32;
     while (cols < 2 * 16 * pairs) cols *= 2;  // mode output + run accumulator
     a.tmem_cols = cols;
-    const bool bf16 = kind == KRONMULT_COMPUTE_BF16;
+    const bool split = kind == KRONMULT_COMPUTE_BF16X3;
+    const bool bf16 = kind == KRONMULT_COMPUTE_BF16 || split;
+    const size_t parts = split ? 2 : 1;
     const size_t need = (size_t)a.N * sizeof(float) +
-                        (bf16 ? (size_t)pairs * kPairBytes + 64 + (size_t)d * kBf16B
+                        (bf16 ? parts * pairs * kPairBytes + 64 + parts * d * kBf16B
                               : (size_t)a.tiles * kTileBytes + 64 + (size_t)2 * d * kBBytes) +
                         32;  // + two mbarriers and the TMEM address
     // resident CTAs per SM are limited so that their tensor-memory columns fit in 512
@@ -749,7 +814,9 @@ int launch_tc_forward(int kind, int d, int n, const float *const *mats, int stri
     smem &= ~(size_t)15;
     if (smem < need) smem = need;
     if (smem > (size_t)di.max_smem_optin) return cudaErrorNotSupported;
-    const void *fn = bf16 ? (const void *)fwd_tc_bf16_kernel : (const void *)fwd_tc_kernel<KIND_TF32>;
+    const void *fn = split  ? (const void *)fwd_tc_bf16_kernel<true>
+                     : bf16 ? (const void *)fwd_tc_bf16_kernel<false>
+                            : (const void *)fwd_tc_kernel<KIND_TF32>;
     if (!ensure_smem_attr(fn, smem)) return cudaErrorInvalidValue;
     // runs of 8 consecutive entries per CTA (the fan-in of a typical output group) and as
     // many CTAs as that gives: the hardware keeps as many resident as the shared-memory
@@ -760,8 +827,10 @@ int launch_tc_forward(int kind, int d, int n, const float *const *mats, int stri
     a.entries_per_cta = (int)ept;
     const long long grid = (nb + ept - 1) / ept;
     if (grid > INT_MAX) return cudaErrorInvalidValue;
-    if (bf16)
-        fwd_tc_bf16_kernel<<<(unsigned)grid, kTcThreads, smem, st>>>(a);
+    if (split)
+        fwd_tc_bf16_kernel<true><<<(unsigned)grid, kTcThreads, smem, st>>>(a);
+    else if (bf16)
+        fwd_tc_bf16_kernel<false><<<(unsigned)grid, kTcThreads, smem, st>>>(a);
     else
         fwd_tc_kernel<KIND_TF32><<<(unsigned)grid, kTcThreads, smem, st>>>(a);
     return (int)cudaGetLastError();

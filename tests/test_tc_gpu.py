@@ -1,9 +1,11 @@
-"""Tensor-core (tcgen05) reduced-precision forward for n = 8: TF32 and BF16 mode
-products with FP32 accumulation and FP64 output accumulation, against the FP64
-oracle.  Errors are stated against FP64 (relative L2):
-  FP32 CUDA-core  <= 1e-6   TF32 tensor core  <= 2e-3   BF16 tensor core  <= 2e-2
-(TF32 keeps 10 mantissa bits, BF16 7; each of the d roundings of the vector and
-of the factors contributes about 2^-11 resp. 2^-8 relative error.)"""
+"""Tensor-core (tcgen05) reduced-precision forward for n = 8: TF32, BF16 and split-BF16
+(BF16X3: v = hi + lo, three MMAs per product) mode products with FP32 accumulation and
+FP64 output accumulation, against the FP64 oracle.  Errors are stated against FP64
+(relative L2):
+  FP32 CUDA-core <= 1e-6   TF32 <= 2e-3   BF16 <= 2e-2   BF16X3 <= 1e-4
+(TF32 keeps 10 mantissa bits, BF16 7, the split pair about 16; each of the d roundings
+of the vector and of the factors contributes about 2^-11, 2^-8 resp. 2^-17 relative
+error, the dropped lo.lo term about 2^-16.)"""
 import numpy as np
 import pytest
 import torch
@@ -12,16 +14,21 @@ from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"fp32": 1e-6, "tf32": 2e-3, "bf16": 2e-2}
+TOL = {"fp32": 1e-6, "tf32": 2e-3, "bf16": 2e-2, "bf16x3": 1e-4}
+
+
+def code_of(compute):
+    from kronmult_gb300 import _lib
+
+    return {"fp32": _lib.KRONMULT_COMPUTE_FP32, "tf32": _lib.KRONMULT_COMPUTE_TF32,
+            "bf16": _lib.KRONMULT_COMPUTE_BF16, "bf16x3": _lib.KRONMULT_COMPUTE_BF16X3}[compute]
 
 
 def run_mode(b, cuda, compute):
     from kronmult_gb300 import DeviceBatch, _lib, forward_f32_f64out
 
-    code = {"fp32": _lib.KRONMULT_COMPUTE_FP32, "tf32": _lib.KRONMULT_COMPUTE_TF32,
-            "bf16": _lib.KRONMULT_COMPUTE_BF16}[compute]
     db = DeviceBatch.from_host(b, device=cuda, dtype=torch.float32, out_dtype=torch.float64)
-    forward_f32_f64out(db, compute=code)
+    forward_f32_f64out(db, compute=code_of(compute))
     torch.cuda.synchronize()
     err = ctypes_device_error()
     assert err == 0, f"device error word {err}"
@@ -38,7 +45,7 @@ def ctypes_device_error():
     return c.value
 
 
-@pytest.mark.parametrize("compute", ["tf32", "bf16"])
+@pytest.mark.parametrize("compute", ["tf32", "bf16", "bf16x3"])
 @pytest.mark.parametrize("d", [1, 2, 3, 4])
 def test_tc_shapes(cuda, compute, d):
     from kronmult_gb300 import workloads as W
@@ -48,7 +55,7 @@ def test_tc_shapes(cuda, compute, d):
     assert O.rel_l2(got, O.forward(b)) <= TOL[compute]
 
 
-@pytest.mark.parametrize("compute", ["fp32", "tf32", "bf16"])
+@pytest.mark.parametrize("compute", ["fp32", "tf32", "bf16", "bf16x3"])
 def test_config4_sample(cuda, compute):
     from kronmult_gb300 import workloads as W
 
@@ -114,7 +121,7 @@ def test_bounded_wait_runs_out_into_an_error_status(cuda):
     assert O.rel_l2(run_mode(b, cuda, "tf32"), O.forward(b)) <= TOL["tf32"]
 
 
-@pytest.mark.parametrize("compute", ["tf32", "bf16"])
+@pytest.mark.parametrize("compute", ["tf32", "bf16", "bf16x3"])
 def test_tc_unaligned_inputs(cuda, compute):
     """Input vectors that do not start on a 16-byte boundary take the element-wise
     staging path (no bulk copy); results as with aligned inputs."""
@@ -129,7 +136,7 @@ def test_tc_unaligned_inputs(cuda, compute):
     shifted[:, 1:] = db.inputs
     k = torch.arange(b.nb, device=cuda, dtype=torch.int64)
     in_ptrs = (shifted.data_ptr() + 4 + k * ((b.N + 1) * 4)).contiguous()
-    code = {"tf32": _lib.KRONMULT_COMPUTE_TF32, "bf16": _lib.KRONMULT_COMPUTE_BF16}[compute]
+    code = code_of(compute)
     st = _lib.lib().kronmult_batched_f32_f64out_async(b.d, b.n, db.mat_ptrs.data_ptr(), b.stride, in_ptrs.data_ptr(),
                                                       db.out_ptrs.data_ptr(), None, b.nb, code, None, None)
     assert st == 0
@@ -138,7 +145,7 @@ def test_tc_unaligned_inputs(cuda, compute):
     assert O.rel_l2(db.outputs.cpu().numpy(), O.forward(b)) <= TOL[compute]
 
 
-@pytest.mark.parametrize("compute", ["tf32", "bf16"])
+@pytest.mark.parametrize("compute", ["tf32", "bf16", "bf16x3"])
 @pytest.mark.parametrize("tuning", [{"ctas_per_sm": 3}, {"ctas_per_sm": 5, "entries_per_team": 3},
                                     {"entries_per_team": 1}])
 def test_tc_launch_shapes(cuda, compute, tuning):
@@ -149,7 +156,7 @@ def test_tc_launch_shapes(cuda, compute, tuning):
     from kronmult_gb300 import DeviceBatch, _lib, forward_f32_f64out
     from kronmult_gb300 import workloads as W
 
-    code = {"tf32": _lib.KRONMULT_COMPUTE_TF32, "bf16": _lib.KRONMULT_COMPUTE_BF16}[compute]
+    code = code_of(compute)
     b = W.config4(scale=24 / 4096)
     outs = []
     for t in (None, tuning):
@@ -160,3 +167,17 @@ def test_tc_launch_shapes(cuda, compute, tuning):
         outs.append(db.outputs.cpu().numpy())
     assert O.rel_l2(outs[1], outs[0]) <= (1e-6 if "entries_per_team" in tuning else 1e-12)
     assert O.rel_l2(outs[0], O.forward(b)) <= TOL[compute]
+
+
+def test_split_bf16_accuracy_between_fp32_and_tf32(cuda):
+    """The split-BF16 products keep about 16 significand bits: on the same batch the
+    error against FP64 is far below TF32's and BF16's and above the FP32 sweep's."""
+    from kronmult_gb300 import workloads as W
+
+    b = W.config4(scale=48 / 4096)
+    ref = O.forward(b)
+    err = {c: O.rel_l2(run_mode(b, cuda, c), ref) for c in ("fp32", "tf32", "bf16", "bf16x3")}
+    assert err["bf16x3"] < err["tf32"] / 10
+    assert err["bf16x3"] < err["bf16"] / 100
+    assert err["fp32"] < err["bf16x3"]
+
