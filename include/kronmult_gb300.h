@@ -61,9 +61,10 @@ extern "C" {
 /* Launch shape override used by the autotuner; zero fields mean "heuristic". */
 typedef struct kronmult_tuning {
     int team_size;        /* threads cooperating on one entry: 8,16,...,512 */
-    int ctas_per_sm;      /* resident CTAs per SM to size the grid for (0 = occupancy); the
-                             tensor-core path reserves shared memory so that at most this many
-                             CTAs are resident (0 = as many as tensor memory allows) */
+    int ctas_per_sm;      /* resident CTAs per SM to size the grid for (0 = occupancy; grouped
+                             plans: at most this many persistent CTAs per SM); the tensor-core
+                             path reserves shared memory so that at most this many CTAs are
+                             resident (0 = as many as tensor memory allows) */
     int entries_per_team; /* contiguous entries one team processes (0 = one wave) */
     int prefetch;         /* 0 = automatic, 1 = one staging slot, 2 = copy the next entry asynchronously,
                              3 = as 2 with modes ping-ponging between vector buffers (n x n factors

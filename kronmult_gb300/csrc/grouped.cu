@@ -397,7 +397,9 @@ int grouped_plan_create(GroupedPlan *&out, const kronmult_group *groups, int n_g
         L.fn = sh.fn;
         L.smem = smem;
         L.block = sh.block;
-        L.grid = di.sms * std::max(1, occupancy((const void *)sh.fn, sh.block, smem));
+        int per_sm = std::max(1, occupancy((const void *)sh.fn, sh.block, smem));
+        if (tunings && tunings[g].ctas_per_sm > 0) per_sm = std::min(per_sm, tunings[g].ctas_per_sm);
+        L.grid = di.sms * per_sm;
         GqArgs &a = L.args;
         a.mats = G.matrix_list_batched;
         a.in = G.input_batched;
