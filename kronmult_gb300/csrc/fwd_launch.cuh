@@ -369,9 +369,24 @@ int plan_forward(FwdPlan<T, TO> &pl, int d, int n, const T *const *mats, int str
                     }
                 }
             }
-            const size_t smem = (size_t)teams * team_elems * sizeof(T);
+            size_t smem = (size_t)teams * team_elems * sizeof(T);
             if (fn && smem <= (size_t)di.max_smem_optin && ensure_smem_attr((const void *)fn, smem)) {
-                const long long grid = (nb + teams - 1) / teams;
+                long long grid = (nb + teams - 1) / teams;
+                // FP64 batches of one wave or less: fewer teams per CTA so that every SM holds
+                // the same number of CTAs (256 CTAs on 152 SMs would give some SMs twice the
+                // entries of others: d = 3, n = 4, 8192 entries)
+                if (sizeof(T) == 8 && !(tune && tune->ctas_per_sm > 0) && grid > di.sms) {
+                    const int occ = occupancy((const void *)fn, teams * ts, smem);
+                    if (grid <= (long long)occ * di.sms) {
+                        const long long k = (grid + di.sms - 1) / di.sms;  // CTAs per SM
+                        const long long t2 = (nb + k * di.sms - 1) / (k * di.sms);
+                        if (t2 >= 1 && t2 < teams) {
+                            teams = (int)t2;
+                            smem = (size_t)teams * team_elems * sizeof(T);
+                            grid = (nb + teams - 1) / teams;
+                        }
+                    }
+                }
                 if (grid <= INT_MAX) {
                     a.team_size = ts;
                     a.teams_per_cta = teams;
