@@ -439,11 +439,24 @@ extern "C" int kronmult_batched_f64_emulated_async(int matrix_count, int matrix_
         a.team_elems = 2 * a.vpad + round_up(2 * d * n * n + d, 4);
         int teams = 256 / ts;
         while (teams > 1 && (size_t)teams * a.team_elems * 4 > (size_t)di.max_smem_optin - 4096) teams /= 2;
-        const size_t smem = (size_t)teams * a.team_elems * 4;
+        size_t smem = (size_t)teams * a.team_elems * 4;
         if (smem <= (size_t)di.max_smem_optin - 4096) {
             if (!ensure_smem_attr((const void *)fn, smem)) return cudaErrorInvalidValue;
+            long long grid = (nb_batch + teams - 1) / teams;
+            // one wave or less: every SM holds the same number of CTAs (as the native planner)
+            if (grid > di.sms) {
+                const int occ = occupancy((const void *)fn, teams * ts, smem);
+                if (grid <= (long long)occ * di.sms) {
+                    const long long k = (grid + di.sms - 1) / di.sms;
+                    const long long t2 = (nb_batch + k * di.sms - 1) / (k * di.sms);
+                    if (t2 >= 1 && t2 < teams) {
+                        teams = (int)t2;
+                        smem = (size_t)teams * a.team_elems * 4;
+                        grid = (nb_batch + teams - 1) / teams;
+                    }
+                }
+            }
             a.teams_per_cta = teams;
-            const long long grid = (nb_batch + teams - 1) / teams;
             fn<<<(unsigned)grid, teams * ts, smem, (cudaStream_t)stream>>>(a);
             return (int)cudaGetLastError();
         }
