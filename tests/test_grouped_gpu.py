@@ -369,3 +369,21 @@ def test_emulated_groups_with_adjoint_and_limits(cuda):
         GroupedPlan(big, arithmetic="emulated")
     with pytest.raises(TypeError):
         GroupedPlan(device_groups([b], cuda, dtype=torch.float32), arithmetic="emulated")
+
+
+def test_ctas_per_sm_caps_the_persistent_grid(cuda):
+    """kronmult_tuning.ctas_per_sm bounds a group's persistent CTAs per SM; the result is
+    unchanged up to summation order."""
+    from kronmult_gb300 import workloads as W
+    from kronmult_gb300.grouped import GroupedPlan
+
+    batches = W.config3(scale=0.01)
+    dbs = device_groups(batches, cuda)
+    sms = torch.cuda.get_device_properties(cuda).multi_processor_count
+    plan = GroupedPlan(dbs, mode="atomic", tunings=[{"ctas_per_sm": 2}] * len(dbs))
+    assert plan.info()["grid"] <= 2 * sms
+    plan.run()
+    torch.cuda.synchronize()
+    for b, db in zip(batches, dbs):
+        assert O.rel_l2(db.outputs.cpu().numpy(), O.forward(b)) <= TOL64
+    plan.close()
