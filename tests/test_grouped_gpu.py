@@ -387,3 +387,29 @@ def test_ctas_per_sm_caps_the_persistent_grid(cuda):
     for b, db in zip(batches, dbs):
         assert O.rel_l2(db.outputs.cpu().numpy(), O.forward(b)) <= TOL64
     plan.close()
+
+
+def test_emulated_deterministic_regroup(cuda):
+    """The double-float plans share the device ordering: after an output table changes in
+    place, regroup + run gives the new assignment, bitwise the same on a second run."""
+    from kronmult_gb300 import workloads as W
+    from kronmult_gb300.grouped import GroupedPlan
+    from kronmult_gb300.workloads import Batch
+
+    b = W.make_batch(3, 6, 6, 30, 7, seed=91)
+    db = device_groups([b], cuda)[0]
+    plan = GroupedPlan([db], mode="deterministic", arithmetic="emulated")
+    perm = np.random.Generator(np.random.PCG64(92)).permutation(b.nb)
+    b2 = Batch(b.name, b.d, b.n, b.stride, b.block, b.factors, b.inputs, b.out_init, b.fac_index, b.out_index[perm])
+    db.out_ptrs.copy_(db.outputs.data_ptr() + torch.from_numpy(b2.out_index).to(cuda) * (db.outputs.shape[1] * 8))
+    torch.cuda.synchronize()
+    outs = []
+    for _ in range(2):
+        db.outputs.zero_()
+        plan.regroup()
+        plan.run()
+        torch.cuda.synchronize()
+        outs.append(db.outputs.clone())
+    assert torch.equal(outs[0], outs[1])
+    assert O.rel_l2(outs[0].cpu().numpy(), O.forward(b2)) <= TOL64
+    plan.close()
