@@ -623,6 +623,279 @@ __global__ void __launch_bounds__(256, 3) fwd_pair_kernel(const FwdArgs<float, T
     team_forward_pairs<TO, NN, QP>(a.mats, a.in, a.out, a.d, a.stride, a.N, e, e_end, buf, fac, buf2, fac2, tm);
 }
 
+// ---- n = 4, d = 6: three modes per pass ------------------------------------------
+//
+// For n = 4 a pass over bi-fibres does 4 FMAs per value per mode against one shared-
+// memory read and write of every value, so two modes per pass leave the shared-memory
+// traffic as large as the FMA work.  Here a lane pair owns a 64-value tri-fibre
+// X[cc][a][b] (the three fastest indices, 4 each) and applies three modes per pass:
+// lane h holds cc = 2h, 2h+1 (32 values), applies mode i to index b and mode i-1 to
+// index a in registers, swaps with its partner half of the results (16 shuffles) so
+// that it holds all four cc for rb = 2h, 2h+1, and applies mode i-2 to index cc.  The
+// results go to their thrice-rotated positions
+//     Z[c3 + 64 (rb + 4 ra + 16 rc)]      (N = 4096, 64 tri-fibres)
+// where three single-mode steps would put them, each the same k-ascending FMA chain from
+// 0 (bitwise the reference float kernel).  Two passes instead of three.
+//
+// Packed FP32 pairs (f2) hold the same element of two fibres, so that a factor value
+// duplicated in both halves multiplies both fibres in one instruction and no value is
+// duplicated in registers: the fibres (cl = 0, 1) for modes b and a, then (rb = 2h,
+// 2h + 1) for mode cc.  Shared-memory layouts: tri-fibre c at 72 c, its half h at +36 h;
+// there value (cl, a, b) at +16 cl + 4 a + b as the input lies (t4_in, staged in 16-byte
+// copies) and at +8 a + 2 b + cl as the first pass writes it (t4_phys, read as pairs by
+// the second); the factors of an entry duplicated,
+// A_i(r, k) at words i*32 + 2 (r + 4 k) + {0, 1}.  Lane pairs are assigned tri-fibres
+// (tri4_c3) so that the half-tri-fibre loads and the scattered stores of a pass are
+// free of bank conflicts.  Lane h = 1 computes mode b's rows in the order r ^ 2, so
+// that the rows each lane keeps and sends sit in the same registers on both lanes.
+__host__ __device__ constexpr int t4_in(int p) { return 72 * (p >> 6) + 36 * ((p >> 5) & 1) + (p & 31); }
+__host__ __device__ constexpr int t4_phys(int p)
+{
+    return 72 * (p >> 6) + 36 * ((p >> 5) & 1) + 8 * ((p >> 2) & 3) + 2 * (p & 3) + ((p >> 4) & 1);
+}
+constexpr int kTri4N = 4096;
+constexpr int kTri4Elems = kTri4N / 64 * 72;  // padded vector
+constexpr int kTri4Fac = 6 * 32;              // duplicated factors of one entry
+
+// tri-fibre of team rank `rank` (h = rank & 1): within a warp, b' = bits 1-2, a' bit 0
+// = bit 3, cl' = bit 4 of the rank; a' bit 1 and the half = the warp index
+__device__ __forceinline__ int tri4_c3(int rank)
+{
+    const int w = rank >> 5;
+    return ((rank >> 1) & 3) + 4 * (((rank >> 3) & 1) + 2 * (w & 1)) + 16 * ((rank >> 4) & 1) + 32 * (w >> 1);
+}
+
+__device__ __forceinline__ float f2_lo(f2 v)
+{
+    float lo, hi;
+    f2_unpack(v, lo, hi);
+    return lo;
+}
+__device__ __forceinline__ float f2_hi(f2 v)
+{
+    float lo, hi;
+    f2_unpack(v, lo, hi);
+    return hi;
+}
+
+template <typename TO>
+__device__ __forceinline__ void flush_tri4(TO *dst, const f2 (&acc)[4][4], int c3, int h)
+{
+#pragma unroll
+    for (int ra = 0; ra < 4; ++ra)
+#pragma unroll
+        for (int rc = 0; rc < 4; ++rc) {
+            TO *o = dst + c3 + 64 * (2 * h + 4 * ra + 16 * rc);
+            atomic_add<TO>(o, (TO)f2_lo(acc[ra][rc]));
+            atomic_add<TO>(o + 64, (TO)f2_hi(acc[ra][rc]));
+        }
+}
+
+template <typename TO>
+__device__ __forceinline__ void team_forward_tri4(const float *const *mats, const float *const *in, TO *const *out,
+                                                  int stride, long long e_begin, long long e_end, float *buf,
+                                                  float *fac, float *buf2, float *fac2, const Team &tm)
+{
+    const int c3 = tri4_c3(tm.rank);
+    const int h = tm.rank & 1;
+    const int src0 = 72 * c3 + 36 * h;             // + 8 a + 4 u: (cl, a, b = 2u, 2u + 1)
+    const int dst0 = t4_phys(c3) + 144 * h;        // + 72 j + 288 ra + 1152 rc
+    const int rowp = 4 * h;                        // word offset of row 2h in a duplicated column
+    const f2 zero2 = f2_pack(0.f, 0.f);
+    // -0 + w == w for every w (signed zeros and NaNs included): a run sum starts at -0
+    const f2 nzero2 = f2_pack(-0.f, -0.f);
+    f2 acc[4][4];  // acc[ra][rc] = run sums of elements (rc, ra, rb = 2h) and (rc, ra, 2h + 1)
+#pragma unroll
+    for (int ra = 0; ra < 4; ++ra)
+#pragma unroll
+        for (int rc = 0; rc < 4; ++rc) acc[ra][rc] = nzero2;
+    TO *cur = nullptr;
+
+    // the next entry's pointers, loaded one entry ahead: its input and (rank < 96) the
+    // factor holding the rank-th of the entry's 96 factor values
+    const float *nsrc = nullptr, *nmat = nullptr;
+    TO *nout = nullptr;  // the output of the entry after the current one
+    auto load_ptrs = [&](long long e) {
+        nsrc = in[e];
+        nout = out[e];
+        nmat = tm.rank < 96 ? mats[e * 6 + (tm.rank >> 4)] : nullptr;
+    };
+    // the input goes in as it lies (t4_in), in 16-byte copies where aligned
+    const int in16 = 72 * (tm.rank >> 4) + 36 * ((tm.rank >> 3) & 1) + 4 * (tm.rank & 7);  // t4_in(4 rank)
+    const int in4 = 72 * (tm.rank >> 6) + 36 * ((tm.rank >> 5) & 1) + (tm.rank & 31);      // t4_in(rank)
+    auto stage = [&](float *dst, float *fdst) {
+        if ((reinterpret_cast<uintptr_t>(nsrc) & 15u) == 0) {
+#pragma unroll
+            for (int m = 0; m < 8; ++m) cp_async<16>(dst + in16 + 576 * m, nsrc + 4 * tm.rank + 512 * m);
+        } else {
+#pragma unroll 8
+            for (int m = 0; m < 32; ++m) cp_async<4>(dst + in4 + 144 * m, nsrc + tm.rank + 128 * m);
+        }
+        if (nmat != nullptr) {  // A_i(r, k), rank = 16 i + 4 k + r, twice
+            const float *g = nmat + (tm.rank & 3) + (size_t)((tm.rank >> 2) & 3) * stride;
+            cp_async<4>(fdst + 2 * tm.rank, g);
+            cp_async<4>(fdst + 2 * tm.rank + 1, g);
+        }
+        cp_async_commit();
+    };
+    TO *o = nullptr;  // the current entry's output
+    if (e_begin < e_end) {
+        load_ptrs(e_begin);
+        stage(buf, fac);
+        o = nout;
+        if (e_begin + 1 < e_end) load_ptrs(e_begin + 1);
+    }
+    for (long long e = e_begin; e < e_end; ++e) {
+        cp_async_wait_all();
+        tm.sync();
+        TO *const o_next = nout;
+        if (e + 1 < e_end) {
+            stage(buf2, fac2);
+            if (e + 2 < e_end) load_ptrs(e + 2);
+        }
+        // a new output: write out the previous run's sums and start the next run
+        if (o != cur) {
+            if (cur != nullptr) {
+                flush_tri4<TO>(cur, acc, c3, h);
+#pragma unroll
+                for (int ra = 0; ra < 4; ++ra)
+#pragma unroll
+                    for (int rc = 0; rc < 4; ++rc) acc[ra][rc] = nzero2;
+            }
+            cur = o;
+        }
+#pragma unroll
+        for (int pass = 0; pass < 2; ++pass) {
+            const float *M2 = fac + (5 - 3 * pass) * 32;  // mode on b
+            const float *M1 = M2 - 32;                    // then on a
+            const float *M0 = M2 - 64;                    // then on cc
+            f2 X[4][4];                                   // X[a][b] = fibres (cl 0, cl 1)
+            if (pass == 0) {  // the input layout: paired here
+#pragma unroll
+                for (int a = 0; a < 4; ++a) {
+                    const float4 v0 = *reinterpret_cast<const float4 *>(buf + src0 + 4 * a);
+                    const float4 v1 = *reinterpret_cast<const float4 *>(buf + src0 + 16 + 4 * a);
+                    X[a][0] = f2_pack(v0.x, v1.x);
+                    X[a][1] = f2_pack(v0.y, v1.y);
+                    X[a][2] = f2_pack(v0.z, v1.z);
+                    X[a][3] = f2_pack(v0.w, v1.w);
+                }
+            } else {  // written paired by the first pass
+#pragma unroll
+                for (int a = 0; a < 4; ++a)
+#pragma unroll
+                    for (int u = 0; u < 2; ++u) {
+                        const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(buf + src0 + 8 * a + 4 * u);
+                        X[a][2 * u] = v.x;
+                        X[a][2 * u + 1] = v.y;
+                    }
+            }
+            // mode on b; Y[a][r] holds row r ^ 2h
+            f2 Y[4][4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int r = 0; r < 4; ++r) Y[a][r] = zero2;
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const ulonglong2 m01 = *reinterpret_cast<const ulonglong2 *>(M2 + 8 * b + rowp);
+                const ulonglong2 m23 = *reinterpret_cast<const ulonglong2 *>(M2 + 8 * b + (rowp ^ 4));
+                const f2 m[4] = {m01.x, m01.y, m23.x, m23.y};
+#pragma unroll
+                for (int a = 0; a < 4; ++a)
+#pragma unroll
+                    for (int r = 0; r < 4; ++r) Y[a][r] = f2_fma(m[r], X[a][b], Y[a][r]);
+            }
+            // mode on a; Z[ra][r] holds rb = r ^ 2h
+            f2 Z[4][4];
+#pragma unroll
+            for (int ra = 0; ra < 4; ++ra)
+#pragma unroll
+                for (int r = 0; r < 4; ++r) Z[ra][r] = zero2;
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                const ulonglong2 m01 = *reinterpret_cast<const ulonglong2 *>(M1 + 8 * a);
+                const ulonglong2 m23 = *reinterpret_cast<const ulonglong2 *>(M1 + 8 * a + 4);
+                const f2 m[4] = {m01.x, m01.y, m23.x, m23.y};
+#pragma unroll
+                for (int ra = 0; ra < 4; ++ra)
+#pragma unroll
+                    for (int r = 0; r < 4; ++r) Z[ra][r] = f2_fma(m[ra], Y[a][r], Z[ra][r]);
+            }
+            // keep Z[ra][j] (rb = 2h + j), send Z[ra][2 + j]; receive the partner's
+            // cc = 2(1 - h) + cl at rb = 2h + j.  V[ra][cc] = fibres (rb 2h, rb 2h + 1)
+            f2 V[4][4];
+#pragma unroll
+            for (int ra = 0; ra < 4; ++ra) {
+                const float s00 = f2_lo(Z[ra][2]), s01 = f2_lo(Z[ra][3]);  // cl 0, j = 0, 1
+                const float s10 = f2_hi(Z[ra][2]), s11 = f2_hi(Z[ra][3]);  // cl 1
+                const f2 r0 = f2_pack(__shfl_xor_sync(0xffffffffu, s00, 1), __shfl_xor_sync(0xffffffffu, s01, 1));
+                const f2 r1 = f2_pack(__shfl_xor_sync(0xffffffffu, s10, 1), __shfl_xor_sync(0xffffffffu, s11, 1));
+                const f2 o0 = f2_pack(f2_lo(Z[ra][0]), f2_lo(Z[ra][1]));
+                const f2 o1 = f2_pack(f2_hi(Z[ra][0]), f2_hi(Z[ra][1]));
+                V[ra][0] = h ? r0 : o0;
+                V[ra][1] = h ? r1 : o1;
+                V[ra][2] = h ? o0 : r0;
+                V[ra][3] = h ? o1 : r1;
+            }
+            // mode on cc, cc ascending
+            f2 W[4][4];  // W[ra][rc]
+#pragma unroll
+            for (int ra = 0; ra < 4; ++ra)
+#pragma unroll
+                for (int rc = 0; rc < 4; ++rc) W[ra][rc] = zero2;
+#pragma unroll
+            for (int cc = 0; cc < 4; ++cc) {
+                const ulonglong2 m01 = *reinterpret_cast<const ulonglong2 *>(M0 + 8 * cc);
+                const ulonglong2 m23 = *reinterpret_cast<const ulonglong2 *>(M0 + 8 * cc + 4);
+                const f2 m[4] = {m01.x, m01.y, m23.x, m23.y};
+#pragma unroll
+                for (int ra = 0; ra < 4; ++ra)
+#pragma unroll
+                    for (int rc = 0; rc < 4; ++rc) W[ra][rc] = f2_fma(m[rc], V[ra][cc], W[ra][rc]);
+            }
+            if (pass == 1) {  // into the run sums
+#pragma unroll
+                for (int ra = 0; ra < 4; ++ra)
+#pragma unroll
+                    for (int rc = 0; rc < 4; ++rc) acc[ra][rc] = f2_add(acc[ra][rc], W[ra][rc]);
+            } else {
+                tm.sync();  // every read of buf for this pass is done
+#pragma unroll
+                for (int ra = 0; ra < 4; ++ra)
+#pragma unroll
+                    for (int rc = 0; rc < 4; ++rc) {
+                        buf[dst0 + 288 * ra + 1152 * rc] = f2_lo(W[ra][rc]);
+                        buf[dst0 + 72 + 288 * ra + 1152 * rc] = f2_hi(W[ra][rc]);
+                    }
+                tm.sync();
+            }
+        }
+        o = o_next;
+        float *t = buf;
+        buf = buf2;
+        buf2 = t;
+        t = fac;
+        fac = fac2;
+        fac2 = t;
+    }
+    if (cur != nullptr) flush_tri4<TO>(cur, acc, c3, h);
+}
+
+template <typename TO> __global__ void __launch_bounds__(128, 4) fwd_tri4_kernel(const FwdArgs<float, TO> a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const Team tm(128);
+    float *buf = reinterpret_cast<float *>(smem_raw);
+    float *fac = buf + kTri4Elems;
+    float *buf2 = fac + kTri4Fac;
+    float *fac2 = buf2 + kTri4Elems;
+    // CTA b runs entries [b nb / G, (b + 1) nb / G) of a grid of G
+    const long long e = (long long)blockIdx.x * a.nb / gridDim.x;
+    const long long e_end = (long long)(blockIdx.x + 1) * a.nb / gridDim.x;
+    team_forward_tri4<TO>(a.mats, a.in, a.out, a.stride, e, e_end, buf, fac, buf2, fac2, tm);
+}
+
 template <typename TO> FwdSmemFn<float, TO> fwd_pair_lookup(int nn, int qp);
 
 }  // namespace kgb
@@ -637,6 +910,7 @@ template <typename TO> FwdSmemFn<float, TO> fwd_pair_lookup(int nn, int qp);
         case 4 * 16 + 1: return fwd_pair_kernel<TO, 4, 1>;                                             \
         case 4 * 16 + 2: return fwd_pair_kernel<TO, 4, 2>;                                             \
         case 8 * 16 + 1: return fwd_pair8_kernel<TO>;                                                  \
+        case 4 * 16 + 3: return fwd_tri4_kernel<TO>; /* d = 6: three modes per pass */                 \
         default: return nullptr;                                                                       \
         }                                                                                              \
     }                                                                                                  \

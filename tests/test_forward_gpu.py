@@ -275,6 +275,56 @@ def test_fp32_two_modes_per_pass(cuda, n, d):
     assert O.rel_l2(got64o, O.forward(b)) <= TOL32
 
 
+def test_fp32_three_modes_per_pass_bitwise(cuda):
+    """FP32 n = 4, d = 6 runs three modes per shared-memory pass (a lane pair per
+    64-value tri-fibre).  With one output per entry its results equal, bit for bit, the
+    one-mode-per-step kernel's (a forced team size selects that one): both are the same
+    k-ascending FMA chains."""
+    from kronmult_gb300 import workloads as W
+
+    b = W.make_batch(6, 4, 7, 50, 1, seed=4646)
+    plain, _ = run(b, cuda, dtype=torch.float32, tuning={"team_size": 128})
+    for tuning in (None, {"entries_per_team": 3}):  # one wave; a grid of 3 entries per CTA
+        got, _ = run(b, cuda, dtype=torch.float32, tuning=tuning)
+        assert np.array_equal(got, plain)
+    assert O.rel_l2(plain, O.forward(b)) <= TOL32
+
+
+@pytest.mark.parametrize("tuning", [None, {"entries_per_team": 1}, {"entries_per_team": 5},
+                                    {"entries_per_team": 64}, {"ctas_per_sm": 1}, {"ctas_per_sm": 7}])
+def test_fp32_three_modes_per_pass_runs(cuda, tuning):
+    """Ragged runs of entries into shared outputs (runs cut by the CTAs' shares of the
+    entries), into FP32 and FP64 outputs: the oracle's FP32 sweep up to FP32 rounding."""
+    from kronmult_gb300 import workloads as W
+
+    b = W.make_batch(6, 4, 4, 9, [1, 7, 3, 12, 1, 2, 9, 4, 6], seed=4747, out_init="normal")
+    ref32 = O.forward(b, dtype=np.float32)
+    got, _ = run(b, cuda, dtype=torch.float32, tuning=tuning)
+    assert O.rel_l2(got, ref32) <= 1e-6
+    got64o, _ = run(b, cuda, dtype=torch.float32, out_dtype=torch.float64, tuning=tuning)
+    assert O.rel_l2(got64o, O.forward(b)) <= TOL32
+
+
+def test_fp32_three_modes_per_pass_unaligned_inputs(cuda):
+    """Input vectors that do not start on a 16-byte boundary are staged value by value:
+    the same bits as the aligned inputs."""
+    from kronmult_gb300 import DeviceBatch, _lib
+    from kronmult_gb300 import workloads as W
+
+    b = W.make_batch(6, 4, 5, 6, 3, seed=4848)
+    want, _ = run(b, cuda, dtype=torch.float32)
+    db = DeviceBatch.from_host(b, device=cuda, dtype=torch.float32)
+    shifted = torch.zeros((b.nb, b.N + 1), dtype=torch.float32, device=cuda)
+    shifted[:, 1:] = db.inputs
+    k = torch.arange(b.nb, device=cuda, dtype=torch.int64)
+    in_ptrs = (shifted.data_ptr() + 4 + k * ((b.N + 1) * 4)).contiguous()
+    st = _lib.lib().kronmult_batched_f32(b.d, b.n, db.mat_ptrs.data_ptr(), b.stride, in_ptrs.data_ptr(),
+                                         db.out_ptrs.data_ptr(), None, b.nb)
+    assert st == 0
+    torch.cuda.synchronize()
+    assert O.rel_l2(db.outputs.cpu().numpy(), want) <= 1e-6
+
+
 @pytest.mark.parametrize("d,n", [(3, 6), (2, 6), (6, 3), (3, 5), (2, 7), (4, 3)])
 def test_fp64_element_mapping(cuda, d, n):
     """FP64 shapes whose fibre count leaves lanes idle take the element-mapped kernel."""
