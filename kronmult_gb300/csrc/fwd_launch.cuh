@@ -406,19 +406,20 @@ int plan_forward(FwdPlan<T, TO> &pl, int d, int n, const T *const *mats, int str
         }
         // FP32, n = 4, d = 6: three modes per shared-memory pass, a lane pair per 64-value
         // tri-fibre (fwd_tri4_kernel), one team of 128 threads per CTA, a grid of about
-        // 8 entries per CTA (measured faster than one wave of CTAs with equal shares:
-        // 0.215 against 0.222 ms on 36864 entries), the entries spread evenly
+        // 6 entries per CTA (36864 entries: 0.207 ms; 8: 0.209 ms; one wave of CTAs with
+        // equal shares of all entries: 3-6 % slower), the entries spread evenly
         if constexpr (sizeof(T) == 4) {
             const bool want_tri4 = !single && n == 4 && d == 6 && !(tune && tune->prefetch == 1) &&
                                    !(tune && tune->team_size > 0);
             if (want_tri4) {
                 auto fn = fwd_pair_lookup<TO>(4, 3);
-                const size_t smem = (size_t)2 * (kTri4Elems + kTri4Fac) * sizeof(T);
+                // two staging slots and the middle buffer: 55.5 KB, 4 CTAs per SM
+                const size_t smem = (size_t)(3 * kTri4Elems + 2 * kTri4Fac) * sizeof(T);
                 if (fn && smem <= (size_t)di.max_smem_optin && ensure_smem_attr((const void *)fn, smem)) {
                     int per_sm = (tune && tune->ctas_per_sm > 0) ? tune->ctas_per_sm
                                                                  : occupancy((const void *)fn, 128, smem);
                     if (per_sm < 1) per_sm = 1;
-                    long long ept = (tune && tune->entries_per_team > 0) ? tune->entries_per_team : 8;
+                    long long ept = (tune && tune->entries_per_team > 0) ? tune->entries_per_team : 6;
                     if (ept * di.sms * per_sm > nb * 2) ept = (nb + (long long)di.sms * per_sm - 1) / ((long long)di.sms * per_sm);
                     if (ept < 1) ept = 1;
                     const long long grid = (nb + ept - 1) / ept;
@@ -426,7 +427,7 @@ int plan_forward(FwdPlan<T, TO> &pl, int d, int n, const T *const *mats, int str
                         a.team_size = 128;
                         a.teams_per_cta = 1;
                         a.entries_per_team = (int)((nb + grid - 1) / grid);  // the largest share
-                        a.team_elems = 2 * (kTri4Elems + kTri4Fac);
+                        a.team_elems = 3 * kTri4Elems + 2 * kTri4Fac;
                         a.vec_pad = kTri4Elems;  // padded layouts (t4_in, t4_phys)
                         a.fac_pad = kTri4Fac;    // factors duplicated
                         a.prefetch = 1;

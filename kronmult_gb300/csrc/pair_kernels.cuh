@@ -694,7 +694,7 @@ __device__ __forceinline__ void flush_tri4(TO *dst, const f2 (&acc)[4][4], int c
 template <typename TO>
 __device__ __forceinline__ void team_forward_tri4(const float *const *mats, const float *const *in, TO *const *out,
                                                   int stride, long long e_begin, long long e_end, float *buf,
-                                                  float *fac, float *buf2, float *fac2, const Team &tm)
+                                                  float *fac, float *buf2, float *fac2, float *mid, const Team &tm)
 {
     const int c3 = tri4_c3(tm.rank);
     const int h = tm.rank & 1;
@@ -785,7 +785,7 @@ __device__ __forceinline__ void team_forward_tri4(const float *const *mats, cons
                 for (int a = 0; a < 4; ++a)
 #pragma unroll
                     for (int u = 0; u < 2; ++u) {
-                        const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(buf + src0 + 8 * a + 4 * u);
+                        const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(mid + src0 + 8 * a + 4 * u);
                         X[a][2 * u] = v.x;
                         X[a][2 * u + 1] = v.y;
                     }
@@ -859,14 +859,13 @@ __device__ __forceinline__ void team_forward_tri4(const float *const *mats, cons
                 for (int ra = 0; ra < 4; ++ra)
 #pragma unroll
                     for (int rc = 0; rc < 4; ++rc) acc[ra][rc] = f2_add(acc[ra][rc], W[ra][rc]);
-            } else {
-                tm.sync();  // every read of buf for this pass is done
+            } else {  // into the middle buffer (its last reads were the previous entry's)
 #pragma unroll
                 for (int ra = 0; ra < 4; ++ra)
 #pragma unroll
                     for (int rc = 0; rc < 4; ++rc) {
-                        buf[dst0 + 288 * ra + 1152 * rc] = f2_lo(W[ra][rc]);
-                        buf[dst0 + 72 + 288 * ra + 1152 * rc] = f2_hi(W[ra][rc]);
+                        mid[dst0 + 288 * ra + 1152 * rc] = f2_lo(W[ra][rc]);
+                        mid[dst0 + 72 + 288 * ra + 1152 * rc] = f2_hi(W[ra][rc]);
                     }
                 tm.sync();
             }
@@ -890,10 +889,11 @@ template <typename TO> __global__ void __launch_bounds__(128, 4) fwd_tri4_kernel
     float *fac = buf + kTri4Elems;
     float *buf2 = fac + kTri4Fac;
     float *fac2 = buf2 + kTri4Elems;
+    float *mid = fac2 + kTri4Fac;  // the first pass's results
     // CTA b runs entries [b nb / G, (b + 1) nb / G) of a grid of G
     const long long e = (long long)blockIdx.x * a.nb / gridDim.x;
     const long long e_end = (long long)(blockIdx.x + 1) * a.nb / gridDim.x;
-    team_forward_tri4<TO>(a.mats, a.in, a.out, a.stride, e, e_end, buf, fac, buf2, fac2, tm);
+    team_forward_tri4<TO>(a.mats, a.in, a.out, a.stride, e, e_end, buf, fac, buf2, fac2, mid, tm);
 }
 
 template <typename TO> FwdSmemFn<float, TO> fwd_pair_lookup(int nn, int qp);
