@@ -635,7 +635,8 @@ __global__ void __launch_bounds__(256, 3) fwd_pair_kernel(const FwdArgs<float, T
 // results go to their thrice-rotated positions
 //     Z[c3 + 64 (rb + 4 ra + 16 rc)]      (N = 4096, 64 tri-fibres)
 // where three single-mode steps would put them, each the same k-ascending FMA chain from
-// 0 (bitwise the reference float kernel).  Two passes instead of three.
+// 0 (bitwise the reference float kernel).  Two passes instead of three; the first
+// writes its results into a middle buffer, so an entry needs two team barriers.
 //
 // Packed FP32 pairs (f2) hold the same element of two fibres, so that a factor value
 // duplicated in both halves multiplies both fibres in one instruction and no value is
@@ -657,8 +658,9 @@ constexpr int kTri4N = 4096;
 constexpr int kTri4Elems = kTri4N / 64 * 72;  // padded vector
 constexpr int kTri4Fac = 6 * 32;              // duplicated factors of one entry
 
-// tri-fibre of team rank `rank` (h = rank & 1): within a warp, b' = bits 1-2, a' bit 0
-// = bit 3, cl' = bit 4 of the rank; a' bit 1 and the half = the warp index
+// tri-fibre c3 = b' + 4 a' + 16 cl' + 32 g of team rank `rank` (h = rank & 1): b' from
+// rank bits 1-2, the low bit of a' from bit 3, cl' from bit 4; the high bit of a' and g
+// from the warp index.  A warp's 32 stores of one result then fall on 32 banks.
 __device__ __forceinline__ int tri4_c3(int rank)
 {
     const int w = rank >> 5;
