@@ -221,7 +221,7 @@ def forward_f32_f64out(b: DeviceBatch, compute: int = _lib.KRONMULT_COMPUTE_FP32
 
 
 def forward_from_host(b: DeviceBatch, h_inputs: torch.Tensor, h_factors: torch.Tensor, h_outputs: torch.Tensor,
-                      chunks: int = 8, streams=None) -> None:
+                      chunks: int = 8, streams=None, last_share: float | None = None) -> None:
     """End-to-end forward for a batch whose data lives in (pinned) host memory.
 
     Copies factors and inputs into the batch's device tensors, runs the forward and
@@ -229,11 +229,14 @@ def forward_from_host(b: DeviceBatch, h_inputs: torch.Tensor, h_factors: torch.T
     output-group boundaries: the host-to-device copy of piece i+1 and the
     device-to-host copy of piece i-1 overlap the forward of piece i.  When the
     factor sets or the outputs are not used in increasing order, the factors are
-    copied before and the outputs after the whole batch instead.  Enqueues only;
-    synchronise with torch.cuda.synchronize()."""
+    copied before and the outputs after the whole batch instead.  With `last_share`
+    the last piece holds that share of the output groups and the others split the
+    rest evenly: the forward and the copy back of the last piece are the part of the
+    step that nothing overlaps.  Enqueues only; synchronise with
+    torch.cuda.synchronize()."""
     dev = b.inputs.device
     s_in, s_cmp, s_out = streams or (torch.cuda.Stream(dev), torch.cuda.Stream(dev), torch.cuda.Stream(dev))
-    plan = _host_pipeline_plan(b, chunks)
+    plan = _host_pipeline_plan(b, chunks, last_share)
     cuts, fac_rows, out_rows, monotone, out_monotone = plan
     nchunks = len(cuts) - 1
     d = b.d
@@ -286,9 +289,10 @@ def forward_from_host_mapped(b: DeviceBatch, h_inputs: torch.Tensor, h_factors: 
     """End-to-end forward whose kernels read the inputs and factors straight from pinned
     host memory over the CPU-GPU link (no staging copy); the outputs are accumulated in
     device memory and copied back piecewise, the copy of piece i overlapping the
-    forward of piece i+1.  On GB300 the copy engines move about 0.2 TB/s host-to-device
-    (the FP64 forward alone streams its inputs at that rate), while the SMs read the
-    inputs over the link with the forward slowed by under 2 %.  Only the last piece's
+    forward of piece i+1.  On GB300 the CPU-GPU link moves about 0.21 TB/s
+    host-to-device, by the copy engines or by loads from the SMs alike, and the FP64
+    forward consumes its inputs at about that rate, so reading them over the link
+    slows it by under 2 % and no copy-in precedes it.  Only the last piece's
     copy back is exposed, so the last piece takes `last_share` of the output groups
     (the others share the rest evenly): on the 36864-entry FP64 batch two pieces split
     9:1 measured 6.74 ms against 6.89 ms for an even split.  `h_inputs` and
