@@ -3,6 +3,8 @@ with the C oracle on seeded batches of every configuration's shape; full-size
 checks through size-independent properties.  Tolerances: relative L2 <= 1e-13
 for FP64 (atomic summation order is the only permitted difference), 1e-5 for
 FP32 against the FP64 result."""
+import functools
+
 import numpy as np
 import pytest
 import torch
@@ -363,7 +365,8 @@ def test_forward_from_host_pipelines(cuda, chunks):
     db = DeviceBatch.from_host(b, device=cuda)
     h_in = torch.from_numpy(b.inputs).pin_memory()
     h_fac = torch.from_numpy(b.factors).pin_memory()
-    for fn in (forward_from_host, forward_from_host_mapped):
+    small_last = functools.partial(forward_from_host, last_share=0.05)
+    for fn in (forward_from_host, forward_from_host_mapped, small_last):
         db.outputs.zero_()
         h_out = torch.full(db.outputs.shape, float("nan"), dtype=torch.float64).pin_memory()
         torch.cuda.synchronize()
